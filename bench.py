@@ -1,0 +1,387 @@
+"""Benchmark: k=50 centred+scaled PCA time-to-tol (1e-5) on the 2,000-gene x
+1.3M-cell, ~10%-dense synthetic count matrix (FP32 values), in the
+FP32+FP64-steps form, with the plain FP64 GPU form and the CPU oracle timed
+beside it.
+
+One step = one full PCA to tolerance (column statistics, deferred centring and
+scaling, the IRLBA restart loop, output assembly). The matrix is ~260M nonzeros,
+larger than L2 (129 MB), so no flush is needed between steps.
+
+Usage:
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun (N > 1) every rank solves its own copy (replicas; the path has no
+data-parallel exchange), the timing is the max over ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k=50 PCA time-to-tol (FP32+FP64-steps vs plain FP64, 1 GB300); SpMV HBM GB/s"
+NUMBER = 50
+TOL = 1e-5
+# Lanczos steps the FP64 method needs to reach tol on this workload (measured
+# with the plain FP64 GPU form, which repeats the oracle's restart count on every
+# case the tests compare). The CPU reference arm times a bounded sample of steps
+# and scales by this count.
+REFERENCE_STEPS_TO_TOL = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cells", type=int, default=1300000)
+    ap.add_argument("--genes", type=int, default=2000)
+    ap.add_argument("--density", type=float, default=0.10)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparator")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-restarts", type=int, default=2, help="restarts in the bounded CPU sample")
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        under = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(under), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def spmv_alg_bytes(rows, cols, nnz, vec_bytes, val_bytes=4, idx_bytes=4):
+    """Algorithmic bytes of one SpMV on the int32-index basis:
+    nnz (val + idx) + (rows + 1) 8-byte pointers + input and output vectors."""
+    return nnz * (val_bytes + idx_bytes) + (rows + 1) * 8 + (rows + cols) * vec_bytes
+
+
+def make_input(args):
+    from cppirlba_gb300 import datagen
+    return datagen.scrna_pca_input(args.genes, args.cells, args.density, args.seed, np.float32, cell_major=False)
+
+
+def cpu_sample(inp, init, restarts, threads):
+    """Bounded CPU sample of the FP64 oracle (CppIrlba's algorithm restated):
+    column statistics plus `restarts` restarts of pca(); returns seconds and
+    Lanczos steps."""
+    import oracle
+    vals64 = inp.val.astype(np.float64)
+    spec = oracle.Spec.sparse(inp.nrow, inp.ncol, vals64, inp.idx, inp.ptr, inp.column_major, threads)
+    t0 = time.perf_counter()
+    r = oracle.pca(spec, True, True, NUMBER, oracle.options(initial=init, convergence_tolerance=TOL),
+                   dense_threads=threads, max_restarts=restarts)
+    dt = time.perf_counter() - t0
+    return dt, r["lanczos_steps"]
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    inp = make_input(args)
+    from cppirlba_gb300 import datagen
+    init = datagen.start_vector(inp.ncol)
+    steps_to_tol = REFERENCE_STEPS_TO_TOL
+    samples = []
+    for i in range(args.warmup + args.steps):
+        dt, steps = cpu_sample(inp, init, args.cpu_restarts, threads)
+        if i >= args.warmup:
+            samples.append(dt / max(steps, 1))
+    per_step = statistics.median(samples)
+    value = per_step * steps_to_tol if steps_to_tol else None
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3 if value else None,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "scrna_csr_2k: %d genes x %d cells, density %.2f, FP32 values; centred+scaled "
+                               "PCA k=%d, tol %.0e" % (args.genes, args.cells, args.density, NUMBER, TOL)},
+        "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                         "sample": "oracle (CppIrlba's algorithm restated in C++, FP64, OpenMP) column stats + "
+                                   "first %d restarts of the PCA per step; seconds per Lanczos step %.4f x %s "
+                                   "Lanczos steps to tol" % (args.cpu_restarts, per_step, steps_to_tol)},
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    world, rank, local = dist_setup()
+    import torch
+    import cppirlba_gb300 as eng
+    from cppirlba_gb300 import datagen
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    eng.load_library()
+    t_gen = time.perf_counter()
+    inp = make_input(args)
+    t_gen = time.perf_counter() - t_gen
+    init = datagen.start_vector(inp.ncol)
+    m, n, nnz = inp.nrow, inp.ncol, inp.nnz
+    opts = eng.Options(initial=init, convergence_tolerance=TOL)
+
+    # Device-resident matrix for the timed value.
+    t_ing = time.perf_counter()
+    mat32 = eng.ParallelSparseMatrix(m, n, inp.val, inp.idx, inp.ptr, inp.column_major,
+                                     form=eng.FORM_FP32_FP64STEPS)
+    t_ing = time.perf_counter() - t_ing
+    lay = mat32.layout()
+    stream = torch.cuda.current_stream()
+    dU = torch.empty(m * NUMBER, dtype=torch.float64, device="cuda")
+    dV = torch.empty(n * NUMBER, dtype=torch.float64, device="cuda")
+    dD = torch.empty(NUMBER, dtype=torch.float64, device="cuda")
+    lib = eng.load_library()
+
+    def solve(matrix, profile=False):
+        """One PCA step on device-resident data: statistics + compute + scores."""
+        keep = []
+        o = opts._to_c(keep)
+        S = np.zeros((NUMBER, m))
+        R = np.zeros((NUMBER, n))
+        var = np.zeros(NUMBER)
+        num = ctypes.c_int64()
+        conv = ctypes.c_int32()
+        iters = ctypes.c_int32()
+        st = eng.Stats()
+        eng.set_profiling(profile)
+        rc = lib.irlba_gb300_pca_device(matrix.handle, 1, 1, NUMBER, ctypes.byref(o), ctypes.c_void_p(dU.data_ptr()),
+                                        ctypes.c_void_p(dV.data_ptr()), ctypes.c_void_p(dD.data_ptr()),
+                                        ctypes.byref(num), ctypes.byref(conv), ctypes.byref(iters),
+                                        ctypes.byref(st), ctypes.c_void_p(stream.cuda_stream))
+        eng.set_profiling(False)
+        eng._check(rc)
+        return {"converged": bool(conv.value), "iterations": iters.value, "stats": eng._stats_dict(st)}
+
+    for _ in range(args.warmup):
+        solve(mat32)
+    clocks = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = eng.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    results = []
+    prof_ms = {k: 0.0 for k in ["spmv_mul", "spmv_adj", "cgs", "restart", "rotate", "other"]}
+    prof_launch = dict(prof_ms)
+    for _ in range(args.steps):
+        results.append(solve(mat32, profile=True))
+        pr = eng.last_profile()
+        for k in prof_ms:
+            prof_ms[k] += pr[k]["ms"]
+            prof_launch[k] += pr[k]["launches"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = eng.launch_count() - launches0
+    clk = clocks.stop()
+    ms_total = max_over_ranks(ev0.elapsed_time(ev1))
+    ms_per_step = ms_total / args.steps
+    D32 = dD.cpu().numpy().copy()
+    last = results[-1]
+
+    # Roofline of the dominant kernel class (the SpMV pair), from the CUDA-event
+    # durations measured inside the timed steps.
+    mul_launch = max(prof_launch["spmv_mul"], 1)
+    adj_launch = max(prof_launch["spmv_adj"], 1)
+    b_mul = spmv_alg_bytes(m, n, nnz, 4)
+    b_adj = spmv_alg_bytes(n, m, nnz, 4)
+    t_mul = prof_ms["spmv_mul"] / mul_launch
+    t_adj = prof_ms["spmv_adj"] / adj_launch
+    peak, peak_kind = load_peaks()
+    gbs_mul = b_mul / (t_mul * 1e-3) / 1e9 if t_mul > 0 else None
+    gbs_adj = b_adj / (t_adj * 1e-3) / 1e9 if t_adj > 0 else None
+    both = (b_mul + b_adj) / ((t_mul + t_adj) * 1e-3) / 1e9 if t_mul + t_adj > 0 else None
+    actual_bytes = nnz * (lay["value_bytes"] + lay["index_bytes_mul"]) + nnz * (lay["value_bytes"] + lay["index_bytes_adj"])
+
+    out = {
+        "metric": METRIC,
+        "value": ms_per_step / 1e3,
+        "unit": "s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (FP64 coefficients, norms, recurrence, restart SVD)",
+        "data": "synthetic (seeded scRNA-like log1p negative-binomial counts; no dataset)",
+        "config": {"workload": "scrna_csr_2k: %d genes x %d cells (CSC cells x genes), density %.2f, nnz %d, "
+                               "FP32 values; centred+scaled PCA k=%d, extra_work 7, tol %.0e" %
+                               (args.genes, args.cells, args.density, nnz, NUMBER, TOL),
+                   "form": "fp32_fp64steps", "l2_flush": "inputs larger than L2 (%.1f GB per SpMV)" % (b_mul / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "converged": last["converged"],
+        "restarts": last["iterations"],
+        "lanczos_steps": last["stats"]["lanczos_steps"],
+        "matvecs": last["stats"]["matvecs"],
+        "gpu_launches": launches,
+        "kernel_ms_per_step": {k: v / args.steps for k, v in prof_ms.items()},
+        "roofline": {"bound": "hbm", "kernel": "spmv (multiply + adjoint, fused centre/scale)",
+                     "achieved": both, "peak": peak, "unit": "GB/s",
+                     "frac": (both / peak) if both else None, "peak_source": peak_kind,
+                     "traffic": None,
+                     "achieved_mul": gbs_mul, "achieved_adj": gbs_adj,
+                     "alg_bytes_per_launch": {"mul": b_mul, "adj": b_adj},
+                     "stored_bytes_per_nnz": {"mul": lay["value_bytes"] + lay["index_bytes_mul"],
+                                              "adj": lay["value_bytes"] + lay["index_bytes_adj"]},
+                     "avg_launch_ms": {"mul": t_mul, "adj": t_adj}},
+        "clocks": clk,
+        "setup_s": {"generate": t_gen, "ingest_fp32": t_ing},
+    }
+
+    # End to end through the public API with host buffers: ingestion (H2D of the
+    # compressed matrix), PCA, D2H of scores, rotation and variances.
+    if not args.no_e2e:
+        e2e_times = []
+        h0, d0 = eng.transfer_bytes()
+        n_e2e = max(1, min(args.steps, 2))
+        for _ in range(n_e2e):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mtmp = eng.ParallelSparseMatrix(m, n, inp.val, inp.idx, inp.ptr, inp.column_major,
+                                            form=eng.FORM_FP32_FP64STEPS)
+            r = eng.pca(mtmp, True, True, NUMBER, opts)
+            mtmp.close()
+            torch.cuda.synchronize()
+            e2e_times.append(time.perf_counter() - t0)
+        h1, d1 = eng.transfer_bytes()
+        e2e = max_over_ranks(statistics.median(e2e_times))
+        out["e2e"] = {"value": e2e, "unit": "s", "h2d_bytes_per_step": (h1 - h0) // n_e2e,
+                      "d2h_bytes_per_step": (d1 - d0) // n_e2e,
+                      "note": "host-side ingestion (transpose + panel layout, all host threads) included"}
+
+    # Plain FP64 GPU form on the same matrix (values promoted to FP64).
+    if not args.no_fp64:
+        vals64 = inp.val.astype(np.float64)
+        mat64 = eng.ParallelSparseMatrix(m, n, vals64, inp.idx, inp.ptr, inp.column_major, form=eng.FORM_FP64)
+        del vals64
+        solve(mat64)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r64 = solve(mat64, profile=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pr64 = eng.last_profile()
+        ms64 = e0.elapsed_time(e1)
+        D64 = dD.cpu().numpy().copy()
+        out["fp64_gpu"] = {"time_to_tol_s": ms64 / 1e3, "restarts": r64["iterations"],
+                           "lanczos_steps": r64["stats"]["lanczos_steps"], "converged": r64["converged"],
+                           "kernel_ms": {k: v["ms"] for k, v in pr64.items()},
+                           "speedup_fp32_form": ms64 / ms_per_step,
+                           "fp32_D_max_rel_err_vs_fp64": float(np.max(np.abs(D32 - D64) / D64))}
+        mat64.close()
+
+    # Bounded CPU sample of the FP64 oracle on the host cores, scaled to time-to-tol.
+    if not args.no_cpu and rank == 0:
+        threads = os.cpu_count() or 1
+        dt, steps = cpu_sample(inp, init, args.cpu_restarts, threads)
+        steps_total = out.get("fp64_gpu", {}).get("lanczos_steps", out["lanczos_steps"])
+        per_step = dt / max(steps, 1)
+        out["cpu_baseline"] = {"value": per_step * steps_total, "unit": "s", "cores": threads, "kind": "port",
+                               "sample": "FP64 oracle (CppIrlba algorithm restated, OpenMP) column stats + first %d "
+                                         "restarts (%d Lanczos steps) in %.2f s, scaled by the %d Lanczos steps the "
+                                         "FP64 method needs to reach tol" % (args.cpu_restarts, steps, dt, steps_total)}
+
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,422 @@
+"""GB300 (sm_103a) IRLBA engine: Python mirror of CppIrlba's interface.
+
+The names follow CppIrlba (irlba::Options, irlba::compute, irlba::compute_simple,
+irlba::pca, irlba::ParallelSparseMatrix, irlba::SimpleMatrix,
+irlba::CenteredMatrix, irlba::ScaledMatrix) and every call goes through the C
+ABI declared in include/irlba_gb300.h. There is no CPU fallback: if the CUDA
+library is missing or no GPU is visible, the calls raise.
+"""
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_lib", "libirlba_gb300.so")
+
+FORM_FP64 = 0
+FORM_FP32_FP64STEPS = 1
+VALUE_F32 = 0
+VALUE_F64 = 1
+
+OK = 0
+ERROR_INVALID_ARGUMENT = 1
+ERROR_CUDA = 2
+ERROR_NUMERICAL = 3
+ERROR_UNSUPPORTED = 4
+
+
+class IrlbaError(RuntimeError):
+    """An engine call failed; `status` is the irlba_gb300_status code."""
+
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [
+        ("invariant_subspace_tolerance", ctypes.c_double),
+        ("convergence_tolerance", ctypes.c_double),
+        ("singular_value_ratio_tolerance", ctypes.c_double),
+        ("extra_work", ctypes.c_int32),
+        ("max_iterations", ctypes.c_int32),
+        ("exact_for_small_matrix", ctypes.c_int32),
+        ("exact_for_large_number", ctypes.c_int32),
+        ("cap_number", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+        ("initial", ctypes.POINTER(ctypes.c_double)),
+        ("initial_size", ctypes.c_int64),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("matvecs", ctypes.c_int64),
+        ("lanczos_steps", ctypes.c_int64),
+        ("restarts", ctypes.c_int64),
+        ("careful_restarts", ctypes.c_int64),
+        ("seconds_total", ctypes.c_double),
+        ("device_ms", ctypes.c_double),
+        ("kernel_launches", ctypes.c_int64),
+    ]
+
+
+_lib = None
+
+
+def library_path():
+    return _LIB_PATH
+
+
+def load_library():
+    """Load the engine (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        from . import build as _build
+        _build.build()
+    lib = ctypes.CDLL(_LIB_PATH)
+    P = ctypes.c_void_p
+    i64, i32, dbl = ctypes.c_int64, ctypes.c_int32, ctypes.c_double
+    pd = ctypes.POINTER(ctypes.c_double)
+    sig = {
+        "irlba_gb300_default_options": (None, [ctypes.POINTER(_Options)]),
+        "irlba_gb300_last_error": (ctypes.c_char_p, []),
+        "irlba_gb300_device_count": (ctypes.c_int, []),
+        "irlba_gb300_matrix_create_sparse": (i32, [i64, i64, P, i32, P, P, i32, i32, ctypes.POINTER(P)]),
+        "irlba_gb300_matrix_create_dense": (i32, [i64, i64, P, i32, i64, i32, i32, ctypes.POINTER(P)]),
+        "irlba_gb300_matrix_center": (i32, [P, pd, ctypes.POINTER(P)]),
+        "irlba_gb300_matrix_scale": (i32, [P, pd, i32, i32, ctypes.POINTER(P)]),
+        "irlba_gb300_matrix_destroy": (i32, [P]),
+        "irlba_gb300_matrix_dims": (i32, [P, ctypes.POINTER(i64), ctypes.POINTER(i64)]),
+        "irlba_gb300_multiply": (i32, [P, pd, pd]),
+        "irlba_gb300_adjoint_multiply": (i32, [P, pd, pd]),
+        "irlba_gb300_realize": (i32, [P, pd]),
+        "irlba_gb300_compute": (i32, [P, i64, ctypes.POINTER(_Options), pd, pd, pd, ctypes.POINTER(i64),
+                                      ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(Stats)]),
+        "irlba_gb300_compute_device": (i32, [P, i64, ctypes.POINTER(_Options), P, P, P, ctypes.POINTER(i64),
+                                             ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(Stats), P]),
+        "irlba_gb300_pca": (i32, [P, i32, i32, i64, ctypes.POINTER(_Options), pd, pd, pd, ctypes.POINTER(i64),
+                                  ctypes.POINTER(i32), ctypes.POINTER(i32), pd, pd, ctypes.POINTER(Stats)]),
+        "irlba_gb300_pca_device": (i32, [P, i32, i32, i64, ctypes.POINTER(_Options), P, P, P, ctypes.POINTER(i64),
+                                         ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(Stats), P]),
+        "irlba_gb300_orthogonalize_vector_device": (i32, [P, i64, i64, i64, P, P]),
+        "irlba_gb300_spmv_device": (i32, [P, i32, P, P, P]),
+        "irlba_gb300_matrix_layout": (i32, [P, ctypes.POINTER(i64), ctypes.POINTER(i32), ctypes.POINTER(i32),
+                                            ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+        "irlba_gb300_set_profiling": (None, [i32]),
+        "irlba_gb300_last_profile": (None, [pd, ctypes.POINTER(i64)]),
+        "irlba_gb300_launch_count": (i64, []),
+        "irlba_gb300_transfer_bytes": (None, [ctypes.POINTER(i64), ctypes.POINTER(i64)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(status):
+    if status != OK:
+        msg = load_library().irlba_gb300_last_error().decode()
+        raise IrlbaError(status, msg)
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _vptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+@dataclass
+class Options:
+    """irlba::Options (Options.hpp:19-83): same field names and defaults."""
+
+    invariant_subspace_tolerance: float = -1.0
+    convergence_tolerance: float = 1e-5
+    singular_value_ratio_tolerance: float = -1.0
+    extra_work: int = 7
+    max_iterations: int = 1000
+    exact_for_small_matrix: bool = True
+    exact_for_large_number: bool = True
+    cap_number: bool = False
+    seed: int = 5489
+    initial: Optional[np.ndarray] = None
+
+    def _to_c(self, keep):
+        o = _Options()
+        o.invariant_subspace_tolerance = self.invariant_subspace_tolerance
+        o.convergence_tolerance = self.convergence_tolerance
+        o.singular_value_ratio_tolerance = self.singular_value_ratio_tolerance
+        o.extra_work = self.extra_work
+        o.max_iterations = self.max_iterations
+        o.exact_for_small_matrix = int(self.exact_for_small_matrix)
+        o.exact_for_large_number = int(self.exact_for_large_number)
+        o.cap_number = int(self.cap_number)
+        o.reserved0 = 0
+        o.seed = self.seed
+        if self.initial is not None:
+            init = np.ascontiguousarray(self.initial, dtype=np.float64)
+            keep.append(init)
+            o.initial = _dptr(init)
+            o.initial_size = init.shape[0]
+        else:
+            o.initial = None
+            o.initial_size = 0
+        return o
+
+
+@dataclass
+class Results:
+    """irlba::Results (compute.hpp:357-388)."""
+
+    U: np.ndarray
+    V: np.ndarray
+    D: np.ndarray
+    iterations: int
+    converged: bool
+    stats: Optional[dict] = None
+
+
+@dataclass
+class PcaResults:
+    """irlba::PcaResults (pca.hpp:146-179)."""
+
+    scores: np.ndarray
+    rotation: np.ndarray
+    variances: np.ndarray
+    iterations: int
+    converged: bool
+    center: Optional[np.ndarray] = None
+    scale: Optional[np.ndarray] = None
+    stats: Optional[dict] = None
+
+
+def _stats_dict(st):
+    return {f: getattr(st, f) for f, _ in Stats._fields_}
+
+
+class Matrix:
+    """irlba::Matrix (Matrix/interface.hpp:141-223) backed by a device handle."""
+
+    def __init__(self, handle, nrow, ncol, form, keep=()):
+        self._h = ctypes.c_void_p(handle)
+        self._nrow = nrow
+        self._ncol = ncol
+        self.form = form
+        self._keep = list(keep)
+
+    def rows(self):
+        return self._nrow
+
+    def cols(self):
+        return self._ncol
+
+    @property
+    def handle(self):
+        return self._h
+
+    def multiply(self, right, output=None):
+        """Workspace::multiply (interface.hpp:49): output = A @ right."""
+        right = np.ascontiguousarray(right, dtype=np.float64)
+        if right.shape != (self._ncol,):
+            raise ValueError("right must have length cols()")
+        out = np.empty(self._nrow) if output is None else output
+        _check(load_library().irlba_gb300_multiply(self._h, _dptr(right), _dptr(out)))
+        return out
+
+    def adjoint_multiply(self, right, output=None):
+        """AdjointWorkspace::multiply (interface.hpp:87): output = A.T @ right."""
+        right = np.ascontiguousarray(right, dtype=np.float64)
+        if right.shape != (self._nrow,):
+            raise ValueError("right must have length rows()")
+        out = np.empty(self._ncol) if output is None else output
+        _check(load_library().irlba_gb300_adjoint_multiply(self._h, _dptr(right), _dptr(out)))
+        return out
+
+    def realize(self):
+        """RealizeWorkspace::realize_copy (interface.hpp:125-130)."""
+        out = np.empty((self._ncol, self._nrow))  # column-major buffer
+        _check(load_library().irlba_gb300_realize(self._h, _dptr(out)))
+        return out.T.copy()
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            load_library().irlba_gb300_matrix_destroy(self._h)
+            self._h = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ParallelSparseMatrix(Matrix):
+    """irlba::ParallelSparseMatrix(nrow, ncol, x, i, p, column_major, num_threads)
+    (Matrix/sparse.hpp:469). num_threads is accepted for interface parity; the
+    device decides its own work split."""
+
+    def __init__(self, nrow, ncol, x, i, p, column_major, num_threads=1, form=FORM_FP64):
+        lib = load_library()
+        x = np.ascontiguousarray(x)
+        if x.dtype not in (np.float32, np.float64):
+            x = x.astype(np.float64)
+        i = np.ascontiguousarray(i, dtype=np.int32)
+        p = np.ascontiguousarray(p, dtype=np.int64)
+        h = ctypes.c_void_p()
+        vt = VALUE_F64 if x.dtype == np.float64 else VALUE_F32
+        _check(lib.irlba_gb300_matrix_create_sparse(nrow, ncol, _vptr(x), vt, _vptr(i), _vptr(p),
+                                                    int(bool(column_major)), form, ctypes.byref(h)))
+        super().__init__(h.value, nrow, ncol, form)
+        self.num_threads = num_threads
+
+    def layout(self):
+        lib = load_library()
+        nnz = ctypes.c_int64()
+        vb, im, ia, pm, pa = (ctypes.c_int32() for _ in range(5))
+        _check(lib.irlba_gb300_matrix_layout(self._h, ctypes.byref(nnz), ctypes.byref(vb), ctypes.byref(im),
+                                             ctypes.byref(ia), ctypes.byref(pm), ctypes.byref(pa)))
+        return {"nnz": nnz.value, "value_bytes": vb.value, "index_bytes_mul": im.value,
+                "index_bytes_adj": ia.value, "panels_mul": pm.value, "panels_adj": pa.value}
+
+
+class SimpleMatrix(Matrix):
+    """irlba::SimpleMatrix over a dense matrix (Matrix/simple.hpp:124-178)."""
+
+    def __init__(self, dense, form=FORM_FP64):
+        lib = load_library()
+        a = np.asarray(dense)
+        if a.dtype not in (np.float32, np.float64):
+            a = a.astype(np.float64)
+        if a.flags.f_contiguous:
+            row_major, buf, ld = 0, a, a.shape[0]
+        else:
+            a = np.ascontiguousarray(a)
+            row_major, buf, ld = 1, a, a.shape[1]
+        h = ctypes.c_void_p()
+        vt = VALUE_F64 if buf.dtype == np.float64 else VALUE_F32
+        _check(lib.irlba_gb300_matrix_create_dense(a.shape[0], a.shape[1], _vptr(buf), vt, max(ld, 1), row_major,
+                                                   form, ctypes.byref(h)))
+        super().__init__(h.value, a.shape[0], a.shape[1], form)
+
+
+class CenteredMatrix(Matrix):
+    """irlba::CenteredMatrix(matrix, center) (Matrix/centered.hpp:152)."""
+
+    def __init__(self, matrix, center):
+        c = np.ascontiguousarray(center, dtype=np.float64)
+        if c.shape != (matrix.cols(),):
+            raise ValueError("center must have length cols()")
+        h = ctypes.c_void_p()
+        _check(load_library().irlba_gb300_matrix_center(matrix.handle, _dptr(c), ctypes.byref(h)))
+        super().__init__(h.value, matrix.rows(), matrix.cols(), matrix.form, keep=[matrix])
+
+
+class ScaledMatrix(Matrix):
+    """irlba::ScaledMatrix(matrix, scale, column, divide) (Matrix/scaled.hpp:420)."""
+
+    def __init__(self, matrix, scale, column, divide):
+        s = np.ascontiguousarray(scale, dtype=np.float64)
+        want = matrix.cols() if column else matrix.rows()
+        if s.shape != (want,):
+            raise ValueError("scale has the wrong length")
+        h = ctypes.c_void_p()
+        _check(load_library().irlba_gb300_matrix_scale(matrix.handle, _dptr(s), int(bool(column)),
+                                                       int(bool(divide)), ctypes.byref(h)))
+        super().__init__(h.value, matrix.rows(), matrix.cols(), matrix.form, keep=[matrix])
+
+
+def compute(matrix, number, options=None):
+    """irlba::compute(matrix, number, options) (compute.hpp:403-410)."""
+    options = options or Options()
+    keep = []
+    o = options._to_c(keep)
+    m, n = matrix.rows(), matrix.cols()
+    cap = max(min(number, min(m, n)), 0)
+    U = np.zeros((cap, m))
+    V = np.zeros((cap, n))
+    D = np.zeros(max(cap, 1))
+    num = ctypes.c_int64()
+    conv = ctypes.c_int32()
+    iters = ctypes.c_int32()
+    st = Stats()
+    _check(load_library().irlba_gb300_compute(matrix.handle, number, ctypes.byref(o), _dptr(U), _dptr(V), _dptr(D),
+                                              ctypes.byref(num), ctypes.byref(conv), ctypes.byref(iters),
+                                              ctypes.byref(st)))
+    r = num.value
+    return Results(U=U[:r].T.copy(), V=V[:r].T.copy(), D=D[:r].copy(), iterations=iters.value,
+                   converged=bool(conv.value), stats=_stats_dict(st))
+
+
+def compute_simple(matrix, number, options=None, form=FORM_FP64):
+    """irlba::compute_simple(matrix, number, options) (compute.hpp:426-433)."""
+    return compute(SimpleMatrix(matrix, form=form), number, options)
+
+
+def pca(matrix, center, scale, number, options=None):
+    """irlba::pca(matrix, center, scale, number, options) (pca.hpp:197-204).
+
+    `matrix` is an undecorated ParallelSparseMatrix or SimpleMatrix (rows are
+    observations, columns are features), or a numpy array (wrapped in a
+    SimpleMatrix)."""
+    if isinstance(matrix, np.ndarray):
+        matrix = SimpleMatrix(matrix)
+    options = options or Options()
+    keep = []
+    o = options._to_c(keep)
+    m, n = matrix.rows(), matrix.cols()
+    cap = max(min(number, min(m, n)), 0)
+    S = np.zeros((cap, m))
+    R = np.zeros((cap, n))
+    var = np.zeros(max(cap, 1))
+    c_out = np.zeros(max(n, 1))
+    s_out = np.zeros(max(n, 1))
+    num = ctypes.c_int64()
+    conv = ctypes.c_int32()
+    iters = ctypes.c_int32()
+    st = Stats()
+    _check(load_library().irlba_gb300_pca(matrix.handle, int(bool(center)), int(bool(scale)), number,
+                                          ctypes.byref(o), _dptr(S), _dptr(R), _dptr(var), ctypes.byref(num),
+                                          ctypes.byref(conv), ctypes.byref(iters), _dptr(c_out), _dptr(s_out),
+                                          ctypes.byref(st)))
+    r = num.value
+    return PcaResults(scores=S[:r].T.copy(), rotation=R[:r].T.copy(), variances=var[:r].copy(),
+                      iterations=iters.value, converged=bool(conv.value),
+                      center=c_out[:n].copy() if center else None, scale=s_out[:n].copy() if scale else None,
+                      stats=_stats_dict(st))
+
+
+def device_count():
+    return load_library().irlba_gb300_device_count()
+
+
+def set_profiling(on):
+    load_library().irlba_gb300_set_profiling(int(bool(on)))
+
+
+def last_profile():
+    ms = (ctypes.c_double * 6)()
+    launches = (ctypes.c_int64 * 6)()
+    load_library().irlba_gb300_last_profile(ms, launches)
+    names = ["spmv_mul", "spmv_adj", "cgs", "restart", "rotate", "other"]
+    return {n: {"ms": ms[i], "launches": launches[i]} for i, n in enumerate(names)}
+
+
+def launch_count():
+    return load_library().irlba_gb300_launch_count()
+
+
+def transfer_bytes():
+    """(host-to-device, device-to-host) bytes copied by the library so far."""
+    h, d = ctypes.c_int64(), ctypes.c_int64()
+    load_library().irlba_gb300_transfer_bytes(ctypes.byref(h), ctypes.byref(d))
+    return h.value, d.value

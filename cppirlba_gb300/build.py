@@ -1,0 +1,80 @@
+"""In-tree build of the GB300 engine (sm_103a) and of the host data generator.
+
+Outputs (git-ignored): cppirlba_gb300/_lib/libirlba_gb300.so and
+cppirlba_gb300/_lib/libirlba_gb300_datagen.so. Translation units compile in
+parallel; nothing here needs a GPU.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_lib")
+BUILD = os.path.join(HERE, "_lib", "obj")
+
+CUDA_SOURCES = ["engine.cu", "spmv.cu", "vec.cu", "svd.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-O3", "-Xcompiler", "-pthread"] + ARCH
+
+
+def _cuda_home():
+    for cand in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if cand and os.path.exists(os.path.join(cand, "bin", "nvcc")):
+            return cand
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(nvcc))
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s" % (" ".join(cmd), res.stdout))
+    return res.stdout
+
+
+def _stale(target, sources):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build(verbose=False, force=False):
+    os.makedirs(BUILD, exist_ok=True)
+    cuda = _cuda_home()
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(HERE, "..", "include", "irlba_gb300.h"))
+
+    lib = os.path.join(OUT, "libirlba_gb300.so")
+    objs = []
+    jobs = []
+    for src in CUDA_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            jobs.append([nvcc] + NVCC_FLAGS + ["-c", s, "-o", o])
+    with ThreadPoolExecutor(max_workers=len(CUDA_SOURCES)) as ex:
+        for out in ex.map(_run, jobs):
+            if verbose and out.strip():
+                print(out)
+    if force or _stale(lib, objs):
+        _run([nvcc] + ARCH + ["-shared", "-cudart", "shared", "-o", lib] + objs +
+             ["-Xlinker", "-rpath," + os.path.join(cuda, "lib64")])
+
+    dg = os.path.join(OUT, "libirlba_gb300_datagen.so")
+    dsrc = os.path.join(CSRC, "datagen.cpp")
+    if force or _stale(dg, [dsrc]):
+        _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread", dsrc, "-o", dg])
+    return lib, dg
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force="--force" in sys.argv))

@@ -1,0 +1,1541 @@
+// Host driver and C ABI of the GB300 IRLBA engine.
+//
+// The restart loop of CppIrlba's irlba::compute (compute.hpp:141-308) runs here
+// with every vector and matrix resident on the device; the host issues the
+// kernels of one restart, then reads a 100-byte control block once per restart
+// (k for the next run, the convergence flag, error flags). Lanczos
+// bidiagonalization (lanczos.hpp:54-143) is issued step by step on one stream.
+// Invariant subspaces (lanczos.hpp:101-106,124-129) are handled by re-running a
+// restart in a careful mode that synchronizes after each norm and draws the
+// random refill from the host engine, in the reference's order.
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/irlba_gb300.h"
+#include "kernels.cuh"
+
+namespace irlba_gb300 {
+
+std::atomic<int64_t> g_launch_count{0};
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+struct Error : public std::runtime_error {
+    irlba_gb300_status status;
+    Error(irlba_gb300_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define CUDA_TRY(expr)                                                                                  \
+    do {                                                                                                \
+        cudaError_t err__ = (expr);                                                                     \
+        if (err__ != cudaSuccess)                                                                       \
+            throw Error(IRLBA_GB300_ERROR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(err__)); \
+    } while (0)
+
+static void invalid(const std::string& m) { throw Error(IRLBA_GB300_ERROR_INVALID_ARGUMENT, m); }
+
+// Host<->device traffic issued by this library (bytes), for end-to-end accounting.
+static std::atomic<int64_t> g_h2d_bytes{0};
+static std::atomic<int64_t> g_d2h_bytes{0};
+
+static cudaError_t h2d_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    g_h2d_bytes.fetch_add(static_cast<int64_t>(bytes));
+    return h2d_async(dst, src, bytes, s);
+}
+static cudaError_t d2h_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    g_d2h_bytes.fetch_add(static_cast<int64_t>(bytes));
+    return d2h_async(dst, src, bytes, s);
+}
+static cudaError_t h2d_sync(void* dst, const void* src, size_t bytes) {
+    g_h2d_bytes.fetch_add(static_cast<int64_t>(bytes));
+    return h2d_sync(dst, src, bytes);
+}
+static cudaError_t d2h_sync(void* dst, const void* src, size_t bytes) {
+    g_d2h_bytes.fetch_add(static_cast<int64_t>(bytes));
+    return d2h_sync(dst, src, bytes);
+}
+
+// ---------------------------------------------------------------------------
+// Device memory
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() {}
+    explicit DevBuf(size_t b) { alloc(b); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : ptr(o.ptr), bytes(o.bytes) { o.ptr = nullptr; o.bytes = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        release();
+        ptr = o.ptr;
+        bytes = o.bytes;
+        o.ptr = nullptr;
+        o.bytes = 0;
+        return *this;
+    }
+    void alloc(size_t b) {
+        release();
+        bytes = b;
+        if (b) CUDA_TRY(cudaMalloc(&ptr, b));
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    ~DevBuf() { release(); }
+    template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+template <typename T>
+static DevBuf upload(const T* host, size_t n) {
+    DevBuf b(sizeof(T) * n);
+    if (n) CUDA_TRY(h2d_sync(b.ptr, host, sizeof(T) * n));
+    return b;
+}
+
+// ---------------------------------------------------------------------------
+// Device properties, configured once per device
+// ---------------------------------------------------------------------------
+// Shared-memory budget for a staged x panel.
+constexpr size_t kPanelBytes = 64 * 1024;
+
+struct DeviceInfo {
+    int device = -1;
+    int sms = 0;
+    size_t max_smem_optin = 0;
+};
+
+static DeviceInfo& device_info() {
+    static thread_local DeviceInfo info;
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (info.device != dev) {
+        cudaDeviceProp prop;
+        CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+        info.device = dev;
+        info.sms = prop.multiProcessorCount;
+        info.max_smem_optin = prop.sharedMemPerBlockOptin;
+        CUDA_TRY(spmv_configure(kPanelBytes));
+        CUDA_TRY(rotate_configure(sizeof(double) * 128 * 128));
+        CUDA_TRY(restart_configure(info.max_smem_optin - 16384));
+        CUDA_TRY(cudaGetLastError());
+    }
+    return info;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side ingestion: compressed matrix -> panel CSR gather plans
+// ---------------------------------------------------------------------------
+static int host_threads() {
+    unsigned n = std::thread::hardware_concurrency();
+    return n == 0 ? 1 : static_cast<int>(std::min(n, 64u));
+}
+
+template <typename F>
+static void parallel_chunks(int64_t n, F f) {
+    const int nt = static_cast<int>(std::min<int64_t>(host_threads(), std::max<int64_t>(1, n / 4096)));
+    if (nt <= 1) {
+        f(0, n, 0);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) {
+        const int64_t b = n * t / nt, e = n * (t + 1) / nt;
+        pool.emplace_back([=, &f]() { f(b, e, t); });
+    }
+    for (auto& th : pool) th.join();
+}
+
+// A compressed gather view on the host: rows x cols, ptr (rows+1), idx, val.
+struct HostCompressed {
+    int64_t rows = 0, cols = 0;
+    const int64_t* ptr = nullptr;
+    const int32_t* idx = nullptr;
+    const void* val = nullptr;
+    bool f64 = false;
+    // Owned storage when produced by a transpose or a dense conversion.
+    std::vector<int64_t> own_ptr;
+    std::vector<int32_t> own_idx;
+    std::vector<float> own_f32;
+    std::vector<double> own_f64;
+};
+
+static double value_at(const HostCompressed& h, int64_t s) {
+    return h.f64 ? static_cast<const double*>(h.val)[s] : static_cast<double>(static_cast<const float*>(h.val)[s]);
+}
+
+// Transpose (counting sort by column, stable in row order), multithreaded.
+static void transpose_host(const HostCompressed& in, HostCompressed& out) {
+    const int64_t R = in.rows, C = in.cols;
+    const int64_t nnz = in.ptr[R];
+    out.rows = C;
+    out.cols = R;
+    out.f64 = in.f64;
+    out.own_ptr.assign(C + 1, 0);
+    out.own_idx.resize(nnz);
+    if (in.f64) out.own_f64.resize(nnz); else out.own_f32.resize(nnz);
+    const int nt = static_cast<int>(std::min<int64_t>(host_threads(), std::max<int64_t>(1, nnz / 65536)));
+    std::vector<std::vector<int64_t>> hist(nt, std::vector<int64_t>(C, 0));
+    auto row_range = [&](int t, int64_t& b, int64_t& e) {
+        b = R * t / nt;
+        e = R * (t + 1) / nt;
+    };
+    {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back([&, t]() {
+                int64_t b, e;
+                row_range(t, b, e);
+                auto& h = hist[t];
+                for (int64_t s = in.ptr[b]; s < in.ptr[e]; ++s) ++h[in.idx[s]];
+            });
+        for (auto& th : pool) th.join();
+    }
+    // Column-major exclusive offsets: column c, thread t.
+    int64_t run = 0;
+    for (int64_t c = 0; c < C; ++c) {
+        out.own_ptr[c] = run;
+        for (int t = 0; t < nt; ++t) {
+            const int64_t v = hist[t][c];
+            hist[t][c] = run;
+            run += v;
+        }
+    }
+    out.own_ptr[C] = run;
+    {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back([&, t]() {
+                int64_t b, e;
+                row_range(t, b, e);
+                auto& h = hist[t];
+                for (int64_t r = b; r < e; ++r)
+                    for (int64_t s = in.ptr[r]; s < in.ptr[r + 1]; ++s) {
+                        const int64_t dst = h[in.idx[s]]++;
+                        out.own_idx[dst] = static_cast<int32_t>(r);
+                        if (in.f64) out.own_f64[dst] = static_cast<const double*>(in.val)[s];
+                        else out.own_f32[dst] = static_cast<const float*>(in.val)[s];
+                    }
+            });
+        for (auto& th : pool) th.join();
+    }
+    out.ptr = out.own_ptr.data();
+    out.idx = out.own_idx.data();
+    out.val = in.f64 ? static_cast<const void*>(out.own_f64.data()) : static_cast<const void*>(out.own_f32.data());
+}
+
+// A device gather plan with the buffers it owns.
+struct DirPlan {
+    DirPlanDev dev;
+    DevBuf segptr, idx, val, block_seg;
+};
+
+// Relative cost of a segment against one nonzero when balancing CTAs.
+constexpr int64_t kSegCost = 8;
+
+static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirPlan& plan) {
+    const DeviceInfo& di = device_info();
+    DirPlanDev& d = plan.dev;
+    d.nrows = h.rows;
+    d.ncols = h.cols;
+    d.nnz = h.ptr[h.rows];
+    d.val_f64 = store_f64 ? 1 : 0;
+    const size_t xbytes = x_f64 ? 8 : 4;
+    const int64_t pw_max = static_cast<int64_t>(kPanelBytes / xbytes);
+    int64_t npanels = 1;
+    bool staged = true;
+    int64_t pw = std::max<int64_t>(1, std::min<int64_t>(h.cols, pw_max));
+    if (h.cols > pw_max) {
+        npanels = (h.cols + pw_max - 1) / pw_max;
+        const double avg = static_cast<double>(d.nnz) / (static_cast<double>(h.rows) * static_cast<double>(npanels));
+        if (avg < 4.0 || npanels > (1 << 20)) {
+            staged = false;
+            npanels = 1;
+        }
+    }
+    d.staged = staged ? 1 : 0;
+    d.npanels = static_cast<int32_t>(npanels);
+    d.panel_width = staged ? pw : h.cols;
+    d.nseg = npanels * h.rows;
+
+    const int64_t R = h.rows, nnz = d.nnz, nseg = d.nseg;
+    std::vector<int64_t> segptr(nseg + 1, 0);
+    std::vector<uint16_t> idx16;
+    std::vector<int32_t> idx32;
+    std::vector<float> v32;
+    std::vector<double> v64;
+    if (store_f64) v64.resize(nnz); else v32.resize(nnz);
+
+    auto put_value = [&](int64_t dst, int64_t src) {
+        if (store_f64) v64[dst] = value_at(h, src);
+        else v32[dst] = h.f64 ? static_cast<float>(static_cast<const double*>(h.val)[src])
+                              : static_cast<const float*>(h.val)[src];
+    };
+
+    if (!staged || npanels == 1) {
+        for (int64_t r = 0; r <= R; ++r) segptr[r] = h.ptr[r];
+        if (staged) idx16.resize(nnz); else idx32.resize(nnz);
+        parallel_chunks(R, [&](int64_t b, int64_t e, int) {
+            for (int64_t s = h.ptr[b]; s < h.ptr[e]; ++s) {
+                if (staged) idx16[s] = static_cast<uint16_t>(h.idx[s]);
+                else idx32[s] = h.idx[s];
+                put_value(s, s);
+            }
+        });
+    } else {
+        // Count entries per (panel, row) then lay segments out panel-major.
+        std::vector<int64_t> cnt(nseg, 0);
+        parallel_chunks(R, [&](int64_t b, int64_t e, int) {
+            for (int64_t r = b; r < e; ++r)
+                for (int64_t s = h.ptr[r]; s < h.ptr[r + 1]; ++s) ++cnt[(h.idx[s] / pw) * R + r];
+        });
+        for (int64_t sg = 0; sg < nseg; ++sg) segptr[sg + 1] = segptr[sg] + cnt[sg];
+        idx16.resize(nnz);
+        parallel_chunks(R, [&](int64_t b, int64_t e, int) {
+            std::vector<int64_t> fill(npanels);
+            for (int64_t r = b; r < e; ++r) {
+                for (int64_t p = 0; p < npanels; ++p) fill[p] = segptr[p * R + r];
+                for (int64_t s = h.ptr[r]; s < h.ptr[r + 1]; ++s) {
+                    const int64_t c = h.idx[s];
+                    const int64_t p = c / pw;
+                    const int64_t dst = fill[p]++;
+                    idx16[dst] = static_cast<uint16_t>(c - p * pw);
+                    put_value(dst, s);
+                }
+            }
+        });
+    }
+
+    // Balance CTAs over segments by cost = nnz + kSegCost per segment.
+    d.smem_bytes = staged ? static_cast<size_t>(d.panel_width) * xbytes : 0;
+    const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes);
+    int64_t nblocks = static_cast<int64_t>(di.sms) * per_sm;
+    const int64_t total_cost = nnz + kSegCost * nseg;
+    nblocks = std::max<int64_t>(1, std::min<int64_t>(nblocks, std::max<int64_t>(1, total_cost / 2048)));
+    std::vector<int64_t> bseg(nblocks + 1, 0);
+    {
+        int64_t s = 0;
+        for (int64_t b = 1; b < nblocks; ++b) {
+            const int64_t target = total_cost * b / nblocks;
+            while (s < nseg && segptr[s] + kSegCost * s < target) ++s;
+            bseg[b] = s;
+        }
+        bseg[nblocks] = nseg;
+    }
+    d.nblocks = static_cast<int32_t>(nblocks);
+
+    plan.segptr = upload(segptr.data(), segptr.size());
+    if (staged) plan.idx = upload(idx16.data(), idx16.size());
+    else plan.idx = upload(idx32.data(), idx32.size());
+    if (store_f64) plan.val = upload(v64.data(), v64.size());
+    else plan.val = upload(v32.data(), v32.size());
+    plan.block_seg = upload(bseg.data(), bseg.size());
+    d.segptr = plan.segptr.as<int64_t>();
+    d.idx16 = staged ? plan.idx.as<uint16_t>() : nullptr;
+    d.idx32 = staged ? nullptr : plan.idx.as<int32_t>();
+    d.val = plan.val.ptr;
+    d.block_seg = plan.block_seg.as<int64_t>();
+}
+
+// ---------------------------------------------------------------------------
+// Matrix handles
+// ---------------------------------------------------------------------------
+struct BaseMatrix {
+    int64_t nrow = 0, ncol = 0;
+    irlba_gb300_form form = IRLBA_GB300_FORM_FP64;
+    bool store_f64 = true;
+    DirPlan mul;  // rows = nrow, x = ncol
+    DirPlan adj;  // rows = ncol, x = nrow
+};
+
+}  // namespace irlba_gb300
+
+struct irlba_gb300_matrix {
+    int kind = 0;  // 0 base, 1 centre, 2 scale
+    const irlba_gb300_matrix* inner = nullptr;
+    std::shared_ptr<irlba_gb300::BaseMatrix> base;
+    std::vector<double> vec;
+    int column = 1, divide = 1;
+    int64_t nrow = 0, ncol = 0;
+    irlba_gb300_form form = IRLBA_GB300_FORM_FP64;
+};
+
+namespace irlba_gb300 {
+
+// Decorator chain flattened for the fused kernels.
+struct Chain {
+    const BaseMatrix* base = nullptr;
+    const std::vector<double>* center = nullptr;
+    const std::vector<double>* scale = nullptr;
+    int scale_column = 1, scale_divide = 1;
+    int center_outer = 0;
+};
+
+static Chain flatten(const irlba_gb300_matrix* m) {
+    std::vector<const irlba_gb300_matrix*> decos;
+    const irlba_gb300_matrix* cur = m;
+    while (cur && cur->kind != 0) {
+        decos.push_back(cur);
+        cur = cur->inner;
+    }
+    if (!cur) invalid("matrix handle has no base matrix");
+    Chain ch;
+    ch.base = cur->base.get();
+    int ncenter = 0, nscale = 0;
+    for (auto* d : decos) (d->kind == 1 ? ncenter : nscale)++;
+    if (ncenter > 1 || nscale > 1)
+        throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
+                    "the GPU engine fuses at most one CenteredMatrix and one ScaledMatrix over a base matrix");
+    for (auto* d : decos) {
+        if (d->kind == 1) ch.center = &d->vec;
+        else {
+            ch.scale = &d->vec;
+            ch.scale_column = d->column;
+            ch.scale_divide = d->divide;
+        }
+    }
+    // decos[0] is outermost.
+    if (ncenter == 1 && nscale == 1) ch.center_outer = (decos[0]->kind == 1) ? 1 : 0;
+    return ch;
+}
+
+// ---------------------------------------------------------------------------
+// Host random normals: std::mt19937_64 with Box-Muller pairs on 53-bit uniforms
+// (stands in for aarand::standard_normal; fill order as utils.hpp:16-37).
+// ---------------------------------------------------------------------------
+static double uniform01(std::mt19937_64& eng) {
+    return (static_cast<double>(eng() >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+}
+
+static void fill_normals(std::vector<double>& v, std::mt19937_64& eng) {
+    const int64_t n = static_cast<int64_t>(v.size());
+    int64_t total = n;
+    const bool odd = total % 2;
+    if (odd) --total;
+    auto pair = [&](double& a, double& b) {
+        const double u1 = uniform01(eng), u2 = uniform01(eng);
+        const double r = std::sqrt(-2.0 * std::log(u1));
+        const double th = 6.283185307179586476925286766559 * u2;
+        a = r * std::cos(th);
+        b = r * std::sin(th);
+    };
+    for (int64_t i = 0; i < total; i += 2) pair(v[i], v[i + 1]);
+    if (odd) {
+        double a, b;
+        pair(a, b);
+        v[total] = a;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Optional per-kernel-class timing with CUDA events on the engine stream.
+// ---------------------------------------------------------------------------
+enum TimeClass { kTSpmvMul = 0, kTSpmvAdj, kTCgs, kTRestart, kTRotate, kTOther, kTNum };
+
+struct Timer {
+    bool on = false;
+    cudaStream_t stream = nullptr;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    int64_t launches[kTNum] = {0};
+    void begin(int cls, cudaEvent_t* out) {
+        launches[cls]++;
+        if (!on) return;
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, stream);
+        marks.push_back({cls, {a, b}});
+        *out = b;
+    }
+    void end(cudaEvent_t e) {
+        if (on) cudaEventRecord(e, stream);
+    }
+    void collect(double* ms) {
+        for (int i = 0; i < kTNum; ++i) ms[i] = 0;
+        for (auto& m : marks) {
+            float t = 0;
+            cudaEventElapsedTime(&t, m.second.first, m.second.second);
+            ms[m.first] += t;
+            cudaEventDestroy(m.second.first);
+            cudaEventDestroy(m.second.second);
+        }
+        marks.clear();
+    }
+};
+
+struct Scoped {
+    Timer& t;
+    cudaEvent_t e = nullptr;
+    Scoped(Timer& tt, int cls) : t(tt) { t.begin(cls, &e); }
+    ~Scoped() {
+        if (e) t.end(e);
+    }
+};
+
+static bool g_profile = false;
+static double g_last_ms[kTNum] = {0};
+static int64_t g_last_launches[kTNum] = {0};
+
+// ---------------------------------------------------------------------------
+// Engine: one compute() call
+// ---------------------------------------------------------------------------
+static int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+template <typename T>
+struct Engine {
+    const Chain& ch;
+    const BaseMatrix& A;
+    cudaStream_t stream;
+    int64_t m, n;        // rows, cols of the operator
+    int64_t ldv, ldw;    // leading dims of V (n x work) and W (m x work)
+    int work = 0;
+    Timer timer;
+
+    // Device buffers.
+    DevBuf V, W, F, Wn, xtmp, partial, part, t, B, BU, BV, BS, prevS, res, svd_scratch, ctrl_buf;
+    DevBuf center_d, scale_d;
+    Ctrl* ctrl = nullptr;
+
+    // Chain vectors in T precision.
+    const T* cvec = nullptr;   // centre (length n)
+    const T* svec = nullptr;   // scale (length n or m)
+
+    Engine(const Chain& c, cudaStream_t s) : ch(c), A(*c.base), stream(s), m(c.base->nrow), n(c.base->ncol) {
+        timer.stream = s;
+        timer.on = g_profile;
+    }
+
+    void upload_chain() {
+        if (ch.center) {
+            std::vector<T> tmp(ch.center->begin(), ch.center->end());
+            center_d = upload(tmp.data(), tmp.size());
+            cvec = center_d.as<T>();
+        }
+        if (ch.scale) {
+            std::vector<T> tmp(ch.scale->begin(), ch.scale->end());
+            scale_d = upload(tmp.data(), tmp.size());
+            svec = scale_d.as<T>();
+        }
+    }
+
+    void alloc_common() {
+        ctrl_buf.alloc(sizeof(Ctrl));
+        ctrl = ctrl_buf.as<Ctrl>();
+        CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), stream));
+        const int64_t Lmax = std::max(m, n);
+        const int64_t pmax = std::max<int64_t>(A.mul.dev.npanels > 1 ? A.mul.dev.npanels * m : 0,
+                                               A.adj.dev.npanels > 1 ? A.adj.dev.npanels * n : 0);
+        partial.alloc(sizeof(T) * std::max<int64_t>(pmax, 1));
+        xtmp.alloc(sizeof(T) * std::max<int64_t>(Lmax, 1));
+        const int64_t wmax = std::max(work, 1);
+        const int64_t part_sz = std::max<int64_t>(static_cast<int64_t>(cgs_dot_grid(Lmax)) * wmax,
+                                                  static_cast<int64_t>(cgs_update_grid(Lmax))) + 64;
+        part.alloc(sizeof(double) * part_sz);
+        t.alloc(sizeof(double) * std::max<int64_t>(wmax, 1));
+    }
+
+    // ---- the fused matvecs ----------------------------------------------------
+    // multiply: y (m) = Op x (n).  beta_mul must already hold the centring scalar.
+    void multiply(const T* x, T* y, const double* alpha, const T* q) {
+        Scoped sc(timer, kTSpmvMul);
+        Epilogue<T> e;
+        const bool col_scale = ch.scale && ch.scale_column;
+        if (ch.center) {
+            e.beta = &ctrl->beta_mul;
+            e.center_after = ch.center_outer;
+        }
+        if (ch.scale && !ch.scale_column) {
+            e.oscale = svec;
+            e.odivide = ch.scale_divide;
+        }
+        e.alpha = alpha;
+        e.q = q;
+        const T* xin = x;
+        if (col_scale) {
+            if (A.mul.dev.staged) {
+                e.iscale = svec;
+                e.idivide = ch.scale_divide;
+            } else {
+                launch_scale_vector<T>(x, svec, ch.scale_divide, n, xtmp.as<T>(), stream);
+                xin = xtmp.as<T>();
+            }
+        }
+        launch_spmv<T>(A.mul.dev, xin, y, partial.as<T>(), e, &ctrl->abort, stream);
+    }
+
+    // adjoint: y (n) = Op^T x (m).  beta_adj must already hold the centring scalar.
+    void adjoint(const T* x, T* y, const double* alpha, const T* q) {
+        Scoped sc(timer, kTSpmvAdj);
+        Epilogue<T> e;
+        const bool row_scale = ch.scale && !ch.scale_column;
+        if (ch.center) {
+            e.beta = &ctrl->beta_adj;
+            e.cvec = cvec;
+            e.center_after = ch.center_outer;
+        }
+        if (ch.scale && ch.scale_column) {
+            e.oscale = svec;
+            e.odivide = ch.scale_divide;
+        }
+        e.alpha = alpha;
+        e.q = q;
+        const T* xin = x;
+        if (row_scale) {
+            if (A.adj.dev.staged) {
+                e.iscale = svec;
+                e.idivide = ch.scale_divide;
+            } else {
+                launch_scale_vector<T>(x, svec, ch.scale_divide, m, xtmp.as<T>(), stream);
+                xin = xtmp.as<T>();
+            }
+        }
+        launch_spmv<T>(A.adj.dev, xin, y, partial.as<T>(), e, &ctrl->abort, stream);
+    }
+
+    // Scale/centre vectors that define the centring scalars.
+    const T* beta_mul_fscale() const { return (ch.scale && ch.scale_column && !ch.center_outer) ? svec : nullptr; }
+    const T* beta_adj_fscale() const { return (ch.scale && !ch.scale_column && !ch.center_outer) ? svec : nullptr; }
+
+    void beta_mul_of(const T* x) {
+        if (!ch.center) return;
+        launch_beta<T>(x, n, beta_mul_fscale(), ch.scale_divide, cvec, &ctrl->beta_mul, part.as<double>(), ctrl,
+                       stream);
+    }
+    void beta_adj_of(const T* x) {
+        if (!ch.center) return;
+        launch_beta<T>(x, m, beta_adj_fscale(), ch.scale_divide, nullptr, &ctrl->beta_adj, part.as<double>(), ctrl,
+                       stream);
+    }
+
+    // Reorthogonalize v against the first c columns of Q; norm -> *norm_out.
+    void cgs(const T* Q, int64_t L, int64_t ldq, int c, T* v, double* norm_out, int check_eps, int check_null) {
+        Scoped sc(timer, kTCgs);
+        if (c > 0) launch_cgs_dot<T>(Q, L, ldq, c, v, part.as<double>(), t.as<double>(), ctrl, stream);
+        launch_cgs_update<T>(Q, L, ldq, c, t.as<double>(), v, part.as<double>(), norm_out, check_eps, check_null,
+                             ctrl, stream);
+    }
+
+    void normalize_F(int j) {
+        Scoped sc(timer, kTOther);
+        launch_normalize<T>(F.as<T>(), n, &ctrl->R_F, Vcol(j + 1), beta_mul_fscale(), ch.scale_divide,
+                            ch.center ? cvec : nullptr, ch.center ? &ctrl->beta_mul : nullptr, part.as<double>(),
+                            B.as<double>(), j + static_cast<int64_t>(j) * work, work, ctrl, stream);
+    }
+    void normalize_W(int j, const double* norm) {
+        Scoped sc(timer, kTOther);
+        launch_normalize<T>(Wn.as<T>(), m, norm, Wcol(j), beta_adj_fscale(), ch.scale_divide, nullptr,
+                            ch.center ? &ctrl->beta_adj : nullptr, part.as<double>(), nullptr, -1, 0, ctrl, stream);
+    }
+
+    T* Vcol(int j) { return V.as<T>() + j * ldv; }
+    T* Wcol(int j) { return W.as<T>() + j * ldw; }
+
+    void sync_ctrl(Ctrl& h) {
+        CUDA_TRY(d2h_async(&h, ctrl, sizeof(Ctrl), stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+    }
+    void set_scalar(double* dptr, double v) {
+        CUDA_TRY(h2d_async(dptr, &v, sizeof(double), stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+    }
+
+    // Replace v (length L) by random normals from the host engine, then
+    // orthogonalize against Q[:, :c] and normalize; the recurrence scalar at
+    // *scalar becomes 0 (lanczos.hpp:101-106, 124-129).
+    void refill(T* v, int64_t L, const T* Q, int64_t ldq, int c, std::mt19937_64& eng, double* scalar, bool is_F,
+                int j) {
+        std::vector<double> r(L);
+        fill_normals(r, eng);
+        std::vector<T> rt(r.begin(), r.end());
+        CUDA_TRY(h2d_async(v, rt.data(), sizeof(T) * L, stream));
+        cgs(Q, L, ldq, c, v, &ctrl->tmp[0], 0, 0);
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        set_scalar(scalar, 0.0);
+        if (is_F) {
+            Scoped sc(timer, kTOther);
+            launch_normalize<T>(F.as<T>(), n, &ctrl->tmp[0], Vcol(j + 1), beta_mul_fscale(), ch.scale_divide,
+                                ch.center ? cvec : nullptr, ch.center ? &ctrl->beta_mul : nullptr, part.as<double>(),
+                                B.as<double>(), j + static_cast<int64_t>(j) * work, work, ctrl, stream);
+        } else {
+            normalize_W(j + 1, &ctrl->tmp[0]);
+        }
+        (void)v;
+    }
+
+    // run_lanczos_bidiagonalization from column `start` (lanczos.hpp:54-143).
+    // Fast mode raises ctrl->invariant and stops on a tiny norm; careful mode
+    // synchronizes after each norm and refills from the host engine.
+    void lanczos(int start, bool careful, std::mt19937_64& eng, int64_t& matvecs) {
+        // W_next = A * V[:, start]
+        beta_mul_of(Vcol(start));
+        multiply(Vcol(start), Wn.as<T>(), nullptr, nullptr);
+        ++matvecs;
+        cgs(W.as<T>(), m, ldw, start, Wn.as<T>(), &ctrl->S, 0, 1);
+        normalize_W(start, &ctrl->S);
+        for (int j = start; j < work; ++j) {
+            // F = A^T W_next - S V[:, j], reorthogonalized against V[:, :j+1]
+            adjoint(Wn.as<T>(), F.as<T>(), &ctrl->S, Vcol(j));
+            ++matvecs;
+            const bool more = j + 1 < work;
+            cgs(V.as<T>(), n, ldv, j + 1, F.as<T>(), more ? &ctrl->R_F : &ctrl->norm_F, more && !careful ? 1 : 0, 0);
+            if (more) {
+                bool refilled = false;
+                if (careful) {
+                    Ctrl h;
+                    sync_ctrl(h);
+                    if (h.R_F < h.eps) {
+                        refill(F.as<T>(), n, V.as<T>(), ldv, j + 1, eng, &ctrl->R_F, true, j);
+                        refilled = true;
+                    }
+                }
+                if (!refilled) normalize_F(j);
+                // W_next = A F - R_F W[:, j], reorthogonalized against W[:, :j+1]
+                multiply(Vcol(j + 1), Wn.as<T>(), &ctrl->R_F, Wcol(j));
+                ++matvecs;
+                cgs(W.as<T>(), m, ldw, j + 1, Wn.as<T>(), &ctrl->S, careful ? 0 : 1, 0);
+                bool refilledW = false;
+                if (careful) {
+                    Ctrl h;
+                    sync_ctrl(h);
+                    if (h.S < h.eps) {
+                        refill(Wn.as<T>(), m, W.as<T>(), ldw, j + 1, eng, &ctrl->S, false, j);
+                        refilledW = true;
+                    }
+                }
+                if (!refilledW) normalize_W(j + 1, &ctrl->S);
+            } else {
+                // B(j, j) = S (lanczos.hpp:140)
+                CUDA_TRY(cudaMemcpyAsync(B.as<double>() + j + static_cast<int64_t>(j) * work, &ctrl->S,
+                                         sizeof(double), cudaMemcpyDeviceToDevice, stream));
+            }
+        }
+    }
+
+    struct Result {
+        bool converged = false;
+        int iterations = 0;
+    };
+
+    // compute.hpp:172-307 with outputs written to device buffers U (m x r), Vout (n x r), D (r).
+    Result run(int64_t requested, const irlba_gb300_options& opt, double* dU, double* dV, double* dD,
+               irlba_gb300_stats* stats) {
+        const int64_t smaller = std::min(m, n);
+        const int64_t w64 = (requested >= smaller) ? smaller : requested + std::min<int64_t>(smaller - requested, opt.extra_work);
+        if (w64 == 0) invalid("number of requested dimensions must be positive");
+        if (w64 > 128)
+            throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
+                        "the GPU engine supports a working subspace (number + extra_work) of at most 128");
+        work = static_cast<int>(w64);
+        ldv = round_up(std::max<int64_t>(n, 1), 32);
+        ldw = round_up(std::max<int64_t>(m, 1), 32);
+
+        const int64_t launches0 = g_launch_count.load();
+        cudaEvent_t ev0, ev1;
+        CUDA_TRY(cudaEventCreate(&ev0));
+        CUDA_TRY(cudaEventCreate(&ev1));
+        CUDA_TRY(cudaEventRecord(ev0, stream));
+        upload_chain();
+        alloc_common();
+        V.alloc(sizeof(T) * ldv * work);
+        W.alloc(sizeof(T) * ldw * work);
+        F.alloc(sizeof(T) * std::max<int64_t>(n, 1));
+        Wn.alloc(sizeof(T) * std::max<int64_t>(m, 1));
+        B.alloc(sizeof(double) * work * work);
+        BU.alloc(sizeof(double) * work * work);
+        BV.alloc(sizeof(double) * work * work);
+        BS.alloc(sizeof(double) * work);
+        prevS.alloc(sizeof(double) * work);
+        res.alloc(sizeof(double) * work);
+        svd_scratch.alloc(sizeof(double) * 2 * work * work);
+        CUDA_TRY(cudaMemsetAsync(V.ptr, 0, V.bytes, stream));
+        CUDA_TRY(cudaMemsetAsync(W.ptr, 0, W.bytes, stream));
+        CUDA_TRY(cudaMemsetAsync(B.ptr, 0, B.bytes, stream));
+        CUDA_TRY(cudaMemsetAsync(BU.ptr, 0, BU.bytes, stream));
+        CUDA_TRY(cudaMemsetAsync(BV.ptr, 0, BV.bytes, stream));
+        CUDA_TRY(cudaMemsetAsync(BS.ptr, 0, BS.bytes, stream));
+        CUDA_TRY(cudaMemsetAsync(prevS.ptr, 0, prevS.bytes, stream));
+
+        // Start vector (compute.hpp:179-190), normalized on the host in FP64.
+        std::mt19937_64 eng(opt.seed);
+        std::vector<double> v0(n);
+        if (opt.initial) {
+            if (opt.initial_size != n) invalid("initialization vector does not have expected number of rows");
+            std::copy(opt.initial, opt.initial + n, v0.begin());
+        } else {
+            fill_normals(v0, eng);
+        }
+        {
+            double s = 0;
+            for (double x : v0) s += x * x;
+            s = std::sqrt(s);
+            for (double& x : v0) x /= s;
+            std::vector<T> vt(v0.begin(), v0.end());
+            CUDA_TRY(h2d_async(V.ptr, vt.data(), sizeof(T) * n, stream));
+        }
+        const double raw_eps = opt.invariant_subspace_tolerance;
+        const double eps = raw_eps < 0 ? std::pow(std::numeric_limits<double>::epsilon(), 0.8) : raw_eps;
+        {
+            Ctrl h;
+            std::memset(&h, 0, sizeof(h));
+            h.eps = eps;
+            CUDA_TRY(h2d_async(ctrl, &h, sizeof(Ctrl), stream));
+        }
+
+        const double tol = opt.convergence_tolerance;
+        const double svtol = opt.singular_value_ratio_tolerance >= 0 ? opt.singular_value_ratio_tolerance : tol;
+        Result out;
+        int iter = 0;
+        int k = 0;
+        int64_t matvecs = 0, steps = 0, careful_restarts = 0;
+        const DeviceInfo& di = device_info();
+        const size_t restart_smem = di.max_smem_optin - 16384;
+
+        auto reset_flags = [&]() {
+            // abort, invariant, null_start back to zero (contiguous int32 fields).
+            CUDA_TRY(cudaMemsetAsync(&ctrl->abort, 0, 3 * sizeof(int32_t), stream));
+        };
+
+        for (; iter < opt.max_iterations; ++iter) {
+            reset_flags();
+            lanczos(k, false, eng, matvecs);
+            RestartArgs ra;
+            ra.B = B.as<double>();
+            ra.BS = BS.as<double>();
+            ra.BU = BU.as<double>();
+            ra.BV = BV.as<double>();
+            ra.prevS = prevS.as<double>();
+            ra.res = res.as<double>();
+            ra.scratch = svd_scratch.as<double>();
+            ra.work = work;
+            ra.k = k;
+            ra.requested = static_cast<int>(requested);
+            ra.iter = iter;
+            ra.tol = tol;
+            ra.svtol = svtol;
+            ra.ctrl = ctrl;
+            {
+                Scoped sc(timer, kTRestart);
+                launch_restart(ra, stream, restart_smem);
+            }
+            Ctrl h;
+            sync_ctrl(h);
+            if (h.null_start) throw Error(IRLBA_GB300_ERROR_NUMERICAL, "starting vector near the null space of the input matrix");
+            if (h.invariant) {
+                ++careful_restarts;
+                reset_flags();
+                lanczos(k, true, eng, matvecs);
+                {
+                    Scoped sc(timer, kTRestart);
+                    launch_restart(ra, stream, restart_smem);
+                }
+                sync_ctrl(h);
+                if (h.null_start) throw Error(IRLBA_GB300_ERROR_NUMERICAL, "starting vector near the null space of the input matrix");
+            }
+            steps += work - k;
+            if (h.converged) {
+                out.converged = true;
+                break;
+            }
+            const int kn = h.k_next;
+            if (kn >= work)
+                throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
+                            "the working subspace (number + extra_work) is too small to restart the iterations");
+            {
+                Scoped sc(timer, kTRotate);
+                // V[:, :kn] = V BV[:, :kn]; V[:, kn] = F / ||F||  (compute.hpp:268-277)
+                launch_rotate<T>(V.as<T>(), n, ldv, work, BV.as<double>(), work, kn, V.as<T>(), ldv, F.as<T>(),
+                                 &ctrl->norm_F, nullptr, stream);
+                // W[:, :kn] = W BU[:, :kn]  (compute.hpp:279-280)
+                launch_rotate<T>(W.as<T>(), m, ldw, work, BU.as<double>(), work, kn, W.as<T>(), ldw, nullptr, nullptr,
+                                 nullptr, stream);
+            }
+            k = kn;
+        }
+        out.iterations = out.converged ? iter + 1 : iter;
+
+        // Output assembly (compute.hpp:298-305).
+        {
+            Scoped sc(timer, kTOther);
+            CUDA_TRY(cudaMemcpyAsync(dD, BS.ptr, sizeof(double) * requested, cudaMemcpyDeviceToDevice, stream));
+            launch_rotate_out<T>(W.as<T>(), m, ldw, work, BU.as<double>(), work, static_cast<int>(requested), dU, m,
+                                 stream);
+            launch_rotate_out<T>(V.as<T>(), n, ldv, work, BV.as<double>(), work, static_cast<int>(requested), dV, n,
+                                 stream);
+        }
+        CUDA_TRY(cudaEventRecord(ev1, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        CUDA_TRY(cudaGetLastError());
+        float dev_ms = 0;
+        cudaEventElapsedTime(&dev_ms, ev0, ev1);
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        if (stats) {
+            stats->device_ms = dev_ms;
+            stats->kernel_launches = g_launch_count.load() - launches0;
+            stats->matvecs = matvecs;
+            stats->lanczos_steps = steps;
+            stats->restarts = iter + (out.converged ? 1 : 0);
+            stats->careful_restarts = careful_restarts;
+        }
+        timer.collect(g_last_ms);
+        for (int i = 0; i < kTNum; ++i) g_last_launches[i] = timer.launches[i];
+        return out;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Realize (dense FP64, column-major m x n) on the device.
+// ---------------------------------------------------------------------------
+static void realize_device(const Chain& ch, double* out, cudaStream_t stream) {
+    const BaseMatrix& A = *ch.base;
+    CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * A.nrow * A.ncol, stream));
+    launch_realize(A.mul.dev, out, A.nrow, 0, stream);
+    DevBuf c, s;
+    if (ch.center) c = upload(ch.center->data(), ch.center->size());
+    if (ch.scale) s = upload(ch.scale->data(), ch.scale->size());
+    launch_realize_ops(out, A.nrow, A.ncol, c.as<double>(), s.as<double>(), ch.scale_column, ch.scale_divide,
+                       ch.center_outer, stream);
+    CUDA_TRY(cudaStreamSynchronize(stream));
+}
+
+__global__ void transpose_kernel(const double* in, int64_t m, int64_t n, double* out) {
+    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < m * n;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = e % m, c = e / m;
+        out[r * n + c] = in[e];
+    }
+}
+
+__global__ void scale_columns_kernel(double* A, int64_t m, int64_t r, const double* d) {
+    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < m * r;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        A[e] *= d[e / m];
+}
+
+// Exact SVD (compute.hpp:30-46) on the device: realize, then one-sided Jacobi.
+static void exact_device(const Chain& ch, int64_t requested, double* dU, double* dV, double* dD,
+                         cudaStream_t stream) {
+    const int64_t m = ch.base->nrow, n = ch.base->ncol;
+    DevBuf dense(sizeof(double) * std::max<int64_t>(m * n, 1));
+    realize_device(ch, dense.as<double>(), stream);
+    const bool tall = m >= n;
+    const int64_t mm = tall ? m : n, nn = tall ? n : m;
+    DevBuf At;
+    const double* Ain = dense.as<double>();
+    if (!tall) {
+        At.alloc(sizeof(double) * m * n);
+        transpose_kernel<<<152 * 8, 256, 0, stream>>>(dense.as<double>(), m, n, At.as<double>()); count_launch();
+        Ain = At.as<double>();
+    }
+    DevBuf U(sizeof(double) * mm * nn), S(sizeof(double) * nn), V(sizeof(double) * nn * nn),
+        scratch(sizeof(double) * (mm * nn + nn * nn)), ctrlb(sizeof(Ctrl));
+    CUDA_TRY(cudaMemsetAsync(ctrlb.ptr, 0, sizeof(Ctrl), stream));
+    launch_dense_svd(Ain, mm, nn, U.as<double>(), S.as<double>(), V.as<double>(), scratch.as<double>(),
+                     ctrlb.as<Ctrl>(), stream);
+    CUDA_TRY(cudaMemcpyAsync(dD, S.ptr, sizeof(double) * requested, cudaMemcpyDeviceToDevice, stream));
+    // tall: A = U S V^T, U is m x n. wide: A^T = U' S V'^T, so U = V' (m x m), V = U' (n x m).
+    const double* Usrc = tall ? U.as<double>() : V.as<double>();
+    const double* Vsrc = tall ? V.as<double>() : U.as<double>();
+    CUDA_TRY(cudaMemcpyAsync(dU, Usrc, sizeof(double) * m * requested, cudaMemcpyDeviceToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(dV, Vsrc, sizeof(double) * n * requested, cudaMemcpyDeviceToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+}
+
+static bool requested_ge_half(int64_t requested, int64_t smaller) {
+    const int64_t half = smaller / 2;
+    if (requested == half) return smaller % 2 == 0;
+    return requested > half;
+}
+
+struct StreamGuard {
+    cudaStream_t s = nullptr;
+    StreamGuard() { CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+    ~StreamGuard() {
+        if (s) cudaStreamDestroy(s);
+    }
+};
+
+// compute() on device outputs. Returns (converged, iterations); *out_number set.
+static std::pair<bool, int> compute_device(const irlba_gb300_matrix* mat, int64_t number,
+                                           const irlba_gb300_options& opt, double* dU, double* dV, double* dD,
+                                           int64_t* out_number, irlba_gb300_stats* stats, cudaStream_t stream) {
+    const Chain ch = flatten(mat);
+    const int64_t m = ch.base->nrow, n = ch.base->ncol;
+    const int64_t smaller = std::min(m, n);
+    int64_t requested = number;
+    if (number < 0) invalid("requested number of singular values must be non-negative");
+    if (requested > smaller) {
+        if (opt.cap_number) requested = smaller;
+        else invalid("requested number of singular values cannot be greater than the smaller matrix dimension");
+    } else if (requested == smaller && !opt.exact_for_large_number) {
+        invalid("requested number of singular values must be less than the smaller matrix dimension for IRLBA iterations");
+    }
+    *out_number = requested;
+    if ((opt.exact_for_small_matrix && smaller < 6) ||
+        (opt.exact_for_large_number && requested_ge_half(requested, smaller))) {
+        exact_device(ch, requested, dU, dV, dD, stream);
+        return {true, 0};
+    }
+    if (ch.base->form == IRLBA_GB300_FORM_FP32_FP64STEPS) {
+        Engine<float> e(ch, stream);
+        auto r = e.run(requested, opt, dU, dV, dD, stats);
+        return {r.converged, r.iterations};
+    } else {
+        Engine<double> e(ch, stream);
+        auto r = e.run(requested, opt, dU, dV, dD, stats);
+        return {r.converged, r.iterations};
+    }
+}
+
+// A single matvec through the chain (Workspace::multiply / AdjointWorkspace::multiply).
+template <typename T>
+static void matvec_device(const Chain& ch, const double* x_host, double* y_host, bool adjoint, cudaStream_t stream) {
+    Engine<T> e(ch, stream);
+    const int64_t m = ch.base->nrow, n = ch.base->ncol;
+    e.work = 1;
+    e.upload_chain();
+    e.alloc_common();
+    const int64_t lin = adjoint ? m : n, lout = adjoint ? n : m;
+    std::vector<T> xin(x_host, x_host + lin);
+    DevBuf xd = upload(xin.data(), xin.size());
+    DevBuf yd(sizeof(T) * std::max<int64_t>(lout, 1));
+    if (adjoint) {
+        e.beta_adj_of(xd.as<T>());
+        e.adjoint(xd.as<T>(), yd.as<T>(), nullptr, nullptr);
+    } else {
+        e.beta_mul_of(xd.as<T>());
+        e.multiply(xd.as<T>(), yd.as<T>(), nullptr, nullptr);
+    }
+    std::vector<T> yh(lout);
+    CUDA_TRY(d2h_async(yh.data(), yd.ptr, sizeof(T) * lout, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    CUDA_TRY(cudaGetLastError());
+    for (int64_t i = 0; i < lout; ++i) y_host[i] = static_cast<double>(yh[i]);
+}
+
+static HostCompressed dense_to_compressed(int64_t nrow, int64_t ncol, const void* values, bool f64, int64_t ld,
+                                          bool row_major, bool by_rows) {
+    // by_rows: rows = matrix rows, cols = matrix columns; else the transpose.
+    HostCompressed h;
+    const int64_t R = by_rows ? nrow : ncol, C = by_rows ? ncol : nrow;
+    h.rows = R;
+    h.cols = C;
+    h.f64 = f64;
+    auto at = [&](int64_t r, int64_t c) -> double {
+        const int64_t i = row_major ? r * ld + c : c * ld + r;
+        return f64 ? static_cast<const double*>(values)[i] : static_cast<double>(static_cast<const float*>(values)[i]);
+    };
+    h.own_ptr.assign(R + 1, 0);
+    for (int64_t r = 0; r < R; ++r) {
+        int64_t cnt = 0;
+        for (int64_t c = 0; c < C; ++c) {
+            const double v = by_rows ? at(r, c) : at(c, r);
+            if (v != 0) {
+                h.own_idx.push_back(static_cast<int32_t>(c));
+                if (f64) h.own_f64.push_back(v); else h.own_f32.push_back(static_cast<float>(v));
+                ++cnt;
+            }
+        }
+        h.own_ptr[r + 1] = h.own_ptr[r] + cnt;
+    }
+    h.ptr = h.own_ptr.data();
+    h.idx = h.own_idx.data();
+    h.val = f64 ? static_cast<const void*>(h.own_f64.data()) : static_cast<const void*>(h.own_f32.data());
+    return h;
+}
+
+__global__ void variances_kernel(double* d, int64_t r, double denom) {
+    for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; j < r;
+         j += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        d[j] = d[j] * d[j] / denom;
+}
+
+// pca() (pca.hpp:55-139) with outputs in device memory. Column statistics are
+// computed on the device (pca.hpp:85-109); the decorator chain is
+// SimpleMatrix -> CenteredMatrix -> ScaledMatrix(column, divide) (pca.hpp:113-126).
+static std::pair<bool, int> pca_device_impl(const irlba_gb300_matrix* matrix, int32_t center, int32_t scale,
+                                            int64_t number, const irlba_gb300_options& opt, double* dScores,
+                                            double* dRot, double* dVar, double* dCenter, double* dScale,
+                                            int64_t* out_number, irlba_gb300_stats* stats, cudaStream_t s) {
+    if (matrix->kind != 0) invalid("pca() takes an undecorated matrix");
+    const int64_t nr = matrix->nrow, nc = matrix->ncol;
+    if (center && nr < 1) invalid("cannot center with no observations");
+    if (scale && nr < 2) invalid("cannot scale with fewer than two observations");
+    std::vector<double> c0, s0;
+    if (center || scale) {
+        DevBuf cd, sd;
+        if (!dCenter) {
+            cd.alloc(sizeof(double) * std::max<int64_t>(nc, 1));
+            dCenter = cd.as<double>();
+        }
+        if (!dScale) {
+            sd.alloc(sizeof(double) * std::max<int64_t>(nc, 1));
+            dScale = sd.as<double>();
+        }
+        DevBuf scratch(sizeof(double) * 4 * std::max<int64_t>(nc, 1));
+        launch_feature_stats(matrix->base->adj.dev, nr, center, scale, dCenter, dScale, scratch.as<double>(), s);
+        if (center) {
+            c0.resize(nc);
+            CUDA_TRY(d2h_async(c0.data(), dCenter, sizeof(double) * nc, s));
+        }
+        if (scale) {
+            s0.resize(nc);
+            CUDA_TRY(d2h_async(s0.data(), dScale, sizeof(double) * nc, s));
+        }
+        CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    irlba_gb300_matrix cm, sm;
+    const irlba_gb300_matrix* top = matrix;
+    if (center) {
+        cm.kind = 1;
+        cm.inner = top;
+        cm.nrow = nr;
+        cm.ncol = nc;
+        cm.form = matrix->form;
+        cm.vec = c0;
+        top = &cm;
+    }
+    if (scale) {
+        sm.kind = 2;
+        sm.inner = top;
+        sm.nrow = nr;
+        sm.ncol = nc;
+        sm.form = matrix->form;
+        sm.column = 1;
+        sm.divide = 1;
+        sm.vec = s0;
+        top = &sm;
+    }
+    auto r = compute_device(top, number, opt, dScores, dRot, dVar, out_number, stats, s);
+    const int64_t num = *out_number;
+    // scores = U diag(D) (pca.hpp:130); variances = D^2 / (nr - 1) if nc > 1 (pca.hpp:131-136).
+    if (num > 0 && nr > 0) {
+        scale_columns_kernel<<<152 * 8, 256, 0, s>>>(dScores, nr, num, dVar);
+        count_launch();
+    }
+    if (num > 0 && nc > 1) {
+        variances_kernel<<<1, 64, 0, s>>>(dVar, num, static_cast<double>(nr - 1));
+        count_launch();
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    CUDA_TRY(cudaGetLastError());
+    return r;
+}
+
+}  // namespace irlba_gb300
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using namespace irlba_gb300;
+
+template <typename F>
+static irlba_gb300_status guarded(F f) {
+    try {
+        f();
+        return IRLBA_GB300_OK;
+    } catch (const Error& e) {
+        g_last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return IRLBA_GB300_ERROR_CUDA;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return IRLBA_GB300_ERROR_INVALID_ARGUMENT;
+    }
+}
+
+extern "C" {
+
+void irlba_gb300_default_options(irlba_gb300_options* o) {
+    o->invariant_subspace_tolerance = -1;
+    o->convergence_tolerance = 1e-5;
+    o->singular_value_ratio_tolerance = -1;
+    o->extra_work = 7;
+    o->max_iterations = 1000;
+    o->exact_for_small_matrix = 1;
+    o->exact_for_large_number = 1;
+    o->cap_number = 0;
+    o->reserved0 = 0;
+    o->seed = std::mt19937_64::default_seed;
+    o->initial = nullptr;
+    o->initial_size = 0;
+}
+
+const char* irlba_gb300_last_error(void) { return g_last_error.c_str(); }
+
+int irlba_gb300_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return n;
+}
+
+irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, const void* values,
+                                                    irlba_gb300_value_type value_type, const int32_t* indices,
+                                                    const int64_t* pointers, int32_t column_major,
+                                                    irlba_gb300_form form, irlba_gb300_matrix** out) {
+    return guarded([&]() {
+        if (!out) invalid("output handle pointer is NULL");
+        if (nrow < 0 || ncol < 0) invalid("matrix dimensions must be non-negative");
+        const int64_t primary = column_major ? ncol : nrow, secondary = column_major ? nrow : ncol;
+        if (!pointers) invalid("pointers must not be NULL");
+        if (pointers[0] != 0) invalid("pointers must start at zero");
+        for (int64_t p = 0; p < primary; ++p)
+            if (pointers[p + 1] < pointers[p]) invalid("pointers must be non-decreasing");
+        const int64_t nnz = pointers[primary];
+        for (int64_t s = 0; s < nnz; ++s)
+            if (indices[s] < 0 || indices[s] >= secondary) invalid("index out of range of the secondary dimension");
+        device_info();
+        auto base = std::make_shared<BaseMatrix>();
+        base->nrow = nrow;
+        base->ncol = ncol;
+        base->form = form;
+        const bool in_f64 = value_type == IRLBA_GB300_VALUE_F64;
+        base->store_f64 = (form == IRLBA_GB300_FORM_FP64) && in_f64;
+        const bool x_f64 = form == IRLBA_GB300_FORM_FP64;
+        HostCompressed native;
+        native.rows = primary;
+        native.cols = secondary;
+        native.ptr = pointers;
+        native.idx = indices;
+        native.val = values;
+        native.f64 = in_f64;
+        HostCompressed trans;
+        transpose_host(native, trans);
+        // native rows = primary. column_major: primary = columns -> adjoint gather.
+        if (column_major) {
+            build_plan(native, base->store_f64, x_f64, base->adj);
+            build_plan(trans, base->store_f64, x_f64, base->mul);
+        } else {
+            build_plan(native, base->store_f64, x_f64, base->mul);
+            build_plan(trans, base->store_f64, x_f64, base->adj);
+        }
+        auto* h = new irlba_gb300_matrix();
+        h->kind = 0;
+        h->base = base;
+        h->nrow = nrow;
+        h->ncol = ncol;
+        h->form = form;
+        *out = h;
+    });
+}
+
+irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, const void* values,
+                                                   irlba_gb300_value_type value_type, int64_t ld, int32_t row_major,
+                                                   irlba_gb300_form form, irlba_gb300_matrix** out) {
+    return guarded([&]() {
+        if (!out) invalid("output handle pointer is NULL");
+        if (nrow < 0 || ncol < 0) invalid("matrix dimensions must be non-negative");
+        if (ld < (row_major ? ncol : nrow)) invalid("leading dimension is smaller than the matrix extent");
+        device_info();
+        auto base = std::make_shared<BaseMatrix>();
+        base->nrow = nrow;
+        base->ncol = ncol;
+        base->form = form;
+        const bool in_f64 = value_type == IRLBA_GB300_VALUE_F64;
+        base->store_f64 = (form == IRLBA_GB300_FORM_FP64) && in_f64;
+        const bool x_f64 = form == IRLBA_GB300_FORM_FP64;
+        HostCompressed byrow = dense_to_compressed(nrow, ncol, values, in_f64, ld, row_major != 0, true);
+        HostCompressed bycol = dense_to_compressed(nrow, ncol, values, in_f64, ld, row_major != 0, false);
+        build_plan(byrow, base->store_f64, x_f64, base->mul);
+        build_plan(bycol, base->store_f64, x_f64, base->adj);
+        auto* h = new irlba_gb300_matrix();
+        h->kind = 0;
+        h->base = base;
+        h->nrow = nrow;
+        h->ncol = ncol;
+        h->form = form;
+        *out = h;
+    });
+}
+
+irlba_gb300_status irlba_gb300_matrix_center(const irlba_gb300_matrix* inner, const double* center,
+                                             irlba_gb300_matrix** out) {
+    return guarded([&]() {
+        if (!inner || !out || !center) invalid("NULL argument");
+        auto* h = new irlba_gb300_matrix();
+        h->kind = 1;
+        h->inner = inner;
+        h->nrow = inner->nrow;
+        h->ncol = inner->ncol;
+        h->form = inner->form;
+        h->vec.assign(center, center + inner->ncol);
+        *out = h;
+    });
+}
+
+irlba_gb300_status irlba_gb300_matrix_scale(const irlba_gb300_matrix* inner, const double* scale, int32_t column,
+                                            int32_t divide, irlba_gb300_matrix** out) {
+    return guarded([&]() {
+        if (!inner || !out || !scale) invalid("NULL argument");
+        auto* h = new irlba_gb300_matrix();
+        h->kind = 2;
+        h->inner = inner;
+        h->nrow = inner->nrow;
+        h->ncol = inner->ncol;
+        h->form = inner->form;
+        h->column = column ? 1 : 0;
+        h->divide = divide ? 1 : 0;
+        const int64_t len = column ? inner->ncol : inner->nrow;
+        h->vec.assign(scale, scale + len);
+        *out = h;
+    });
+}
+
+irlba_gb300_status irlba_gb300_matrix_destroy(irlba_gb300_matrix* matrix) {
+    return guarded([&]() { delete matrix; });
+}
+
+irlba_gb300_status irlba_gb300_matrix_dims(const irlba_gb300_matrix* matrix, int64_t* nrow, int64_t* ncol) {
+    return guarded([&]() {
+        if (!matrix) invalid("NULL matrix");
+        *nrow = matrix->nrow;
+        *ncol = matrix->ncol;
+    });
+}
+
+irlba_gb300_status irlba_gb300_multiply(const irlba_gb300_matrix* matrix, const double* right, double* output) {
+    return guarded([&]() {
+        const Chain ch = flatten(matrix);
+        StreamGuard sg;
+        if (ch.base->form == IRLBA_GB300_FORM_FP32_FP64STEPS) matvec_device<float>(ch, right, output, false, sg.s);
+        else matvec_device<double>(ch, right, output, false, sg.s);
+    });
+}
+
+irlba_gb300_status irlba_gb300_adjoint_multiply(const irlba_gb300_matrix* matrix, const double* right,
+                                                double* output) {
+    return guarded([&]() {
+        const Chain ch = flatten(matrix);
+        StreamGuard sg;
+        if (ch.base->form == IRLBA_GB300_FORM_FP32_FP64STEPS) matvec_device<float>(ch, right, output, true, sg.s);
+        else matvec_device<double>(ch, right, output, true, sg.s);
+    });
+}
+
+irlba_gb300_status irlba_gb300_realize(const irlba_gb300_matrix* matrix, double* output) {
+    return guarded([&]() {
+        const Chain ch = flatten(matrix);
+        StreamGuard sg;
+        const int64_t total = ch.base->nrow * ch.base->ncol;
+        DevBuf d(sizeof(double) * std::max<int64_t>(total, 1));
+        realize_device(ch, d.as<double>(), sg.s);
+        CUDA_TRY(d2h_sync(output, d.ptr, sizeof(double) * total));
+    });
+}
+
+irlba_gb300_status irlba_gb300_compute(const irlba_gb300_matrix* matrix, int64_t number,
+                                       const irlba_gb300_options* options, double* U, double* V, double* D,
+                                       int64_t* out_number, int32_t* converged, int32_t* iterations,
+                                       irlba_gb300_stats* stats) {
+    return guarded([&]() {
+        if (!matrix) invalid("NULL matrix");
+        irlba_gb300_options opt;
+        if (options) opt = *options; else irlba_gb300_default_options(&opt);
+        auto t0 = std::chrono::steady_clock::now();
+        StreamGuard sg;
+        const int64_t m = matrix->nrow, n = matrix->ncol;
+        const int64_t cap = std::max<int64_t>(std::min(number, std::min(m, n)), 0);
+        DevBuf dU(sizeof(double) * std::max<int64_t>(m * cap, 1)), dV(sizeof(double) * std::max<int64_t>(n * cap, 1)),
+            dD(sizeof(double) * std::max<int64_t>(cap, 1));
+        int64_t num = 0;
+        auto r = compute_device(matrix, number, opt, dU.as<double>(), dV.as<double>(), dD.as<double>(), &num, stats,
+                                sg.s);
+        CUDA_TRY(d2h_sync(U, dU.ptr, sizeof(double) * m * num));
+        CUDA_TRY(d2h_sync(V, dV.ptr, sizeof(double) * n * num));
+        CUDA_TRY(d2h_sync(D, dD.ptr, sizeof(double) * num));
+        if (out_number) *out_number = num;
+        if (converged) *converged = r.first ? 1 : 0;
+        if (iterations) *iterations = r.second;
+        if (stats) stats->seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+}
+
+// Same as irlba_gb300_compute with U, V, D in device memory (sized for `number`).
+irlba_gb300_status irlba_gb300_compute_device(const irlba_gb300_matrix* matrix, int64_t number,
+                                              const irlba_gb300_options* options, double* U_device,
+                                              double* V_device, double* D_device, int64_t* out_number,
+                                              int32_t* converged, int32_t* iterations, irlba_gb300_stats* stats,
+                                              void* stream) {
+    return guarded([&]() {
+        if (!matrix) invalid("NULL matrix");
+        irlba_gb300_options opt;
+        if (options) opt = *options; else irlba_gb300_default_options(&opt);
+        auto t0 = std::chrono::steady_clock::now();
+        std::unique_ptr<StreamGuard> own;
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (!s) {
+            own.reset(new StreamGuard());
+            s = own->s;
+        }
+        int64_t num = 0;
+        auto r = compute_device(matrix, number, opt, U_device, V_device, D_device, &num, stats, s);
+        if (out_number) *out_number = num;
+        if (converged) *converged = r.first ? 1 : 0;
+        if (iterations) *iterations = r.second;
+        if (stats) stats->seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+}
+
+irlba_gb300_status irlba_gb300_pca(const irlba_gb300_matrix* matrix, int32_t center, int32_t scale, int64_t number,
+                                   const irlba_gb300_options* options, double* scores, double* rotation,
+                                   double* variances, int64_t* out_number, int32_t* converged, int32_t* iterations,
+                                   double* center_out, double* scale_out, irlba_gb300_stats* stats) {
+    return guarded([&]() {
+        if (!matrix) invalid("NULL matrix");
+        irlba_gb300_options opt;
+        if (options) opt = *options; else irlba_gb300_default_options(&opt);
+        auto t0 = std::chrono::steady_clock::now();
+        const int64_t nr = matrix->nrow, nc = matrix->ncol;
+        StreamGuard sg;
+        const int64_t cap = std::max<int64_t>(std::min(number, std::min(nr, nc)), 0);
+        DevBuf dS(sizeof(double) * std::max<int64_t>(nr * cap, 1)), dR(sizeof(double) * std::max<int64_t>(nc * cap, 1)),
+            dVar(sizeof(double) * std::max<int64_t>(cap, 1)), dC(sizeof(double) * std::max<int64_t>(nc, 1)),
+            dSc(sizeof(double) * std::max<int64_t>(nc, 1));
+        int64_t num = 0;
+        auto r = pca_device_impl(matrix, center, scale, number, opt, dS.as<double>(), dR.as<double>(),
+                                 dVar.as<double>(), dC.as<double>(), dSc.as<double>(), &num, stats, sg.s);
+        CUDA_TRY(d2h_sync(scores, dS.ptr, sizeof(double) * nr * num));
+        CUDA_TRY(d2h_sync(rotation, dR.ptr, sizeof(double) * nc * num));
+        CUDA_TRY(d2h_sync(variances, dVar.ptr, sizeof(double) * num));
+        if (center_out && center) CUDA_TRY(d2h_sync(center_out, dC.ptr, sizeof(double) * nc));
+        if (scale_out && scale) CUDA_TRY(d2h_sync(scale_out, dSc.ptr, sizeof(double) * nc));
+        if (out_number) *out_number = num;
+        if (converged) *converged = r.first ? 1 : 0;
+        if (iterations) *iterations = r.second;
+        if (stats) stats->seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+}
+
+irlba_gb300_status irlba_gb300_pca_device(const irlba_gb300_matrix* matrix, int32_t center, int32_t scale,
+                                          int64_t number, const irlba_gb300_options* options, double* scores_device,
+                                          double* rotation_device, double* variances_device, int64_t* out_number,
+                                          int32_t* converged, int32_t* iterations, irlba_gb300_stats* stats,
+                                          void* stream) {
+    return guarded([&]() {
+        if (!matrix) invalid("NULL matrix");
+        irlba_gb300_options opt;
+        if (options) opt = *options; else irlba_gb300_default_options(&opt);
+        auto t0 = std::chrono::steady_clock::now();
+        std::unique_ptr<StreamGuard> own;
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (!s) {
+            own.reset(new StreamGuard());
+            s = own->s;
+        }
+        int64_t num = 0;
+        auto r = pca_device_impl(matrix, center, scale, number, opt, scores_device, rotation_device,
+                                 variances_device, nullptr, nullptr, &num, stats, s);
+        if (out_number) *out_number = num;
+        if (converged) *converged = r.first ? 1 : 0;
+        if (iterations) *iterations = r.second;
+        if (stats) stats->seconds_total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+}
+
+irlba_gb300_status irlba_gb300_orthogonalize_vector_device(const double* Q, int64_t L, int64_t ldq, int64_t ncols,
+                                                           double* vec, void* stream) {
+    return guarded([&]() {
+        if (ncols < 0 || ncols > 1024) invalid("ncols must be in [0, 1024]");
+        if (ldq < L) invalid("ldq is smaller than L");
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const int64_t part_sz = std::max<int64_t>(static_cast<int64_t>(cgs_dot_grid(L)) * std::max<int64_t>(ncols, 1),
+                                                  cgs_update_grid(L)) + 64;
+        DevBuf part(sizeof(double) * part_sz), t(sizeof(double) * std::max<int64_t>(ncols, 1)),
+            ctrlb(sizeof(Ctrl)), nrm(sizeof(double));
+        CUDA_TRY(cudaMemsetAsync(ctrlb.ptr, 0, sizeof(Ctrl), s));
+        if (ncols > 0) {
+            launch_cgs_dot<double>(Q, L, ldq, static_cast<int32_t>(ncols), vec, part.as<double>(), t.as<double>(),
+                                   ctrlb.as<Ctrl>(), s);
+            launch_cgs_update<double>(Q, L, ldq, static_cast<int32_t>(ncols), t.as<double>(), vec, part.as<double>(),
+                                      nrm.as<double>(), 0, 0, ctrlb.as<Ctrl>(), s);
+        }
+        CUDA_TRY(cudaStreamSynchronize(s));
+        CUDA_TRY(cudaGetLastError());
+    });
+}
+
+// Per-kernel-class timing of the last compute call (ms) when profiling is on.
+// Classes: 0 SpMV multiply, 1 SpMV adjoint, 2 reorthogonalization,
+// 3 restart (small SVD), 4 rotation, 5 other. launches may be NULL.
+void irlba_gb300_set_profiling(int32_t on) { g_profile = on != 0; }
+int64_t irlba_gb300_launch_count(void) { return g_launch_count.load(); }
+void irlba_gb300_transfer_bytes(int64_t* h2d, int64_t* d2h) {
+    if (h2d) *h2d = g_h2d_bytes.load();
+    if (d2h) *d2h = g_d2h_bytes.load();
+}
+void irlba_gb300_last_profile(double* ms, int64_t* launches) {
+    for (int i = 0; i < kTNum; ++i) {
+        if (ms) ms[i] = g_last_ms[i];
+        if (launches) launches[i] = g_last_launches[i];
+    }
+}
+
+// Single-direction SpMV of a base matrix on device vectors (no centring or
+// scaling), for bandwidth measurement: y = A x (adjoint = 0) or A^T x. Vectors
+// are FP64 for FP64-form matrices and FP32 otherwise.
+irlba_gb300_status irlba_gb300_spmv_device(const irlba_gb300_matrix* matrix, int32_t adjoint, const void* x,
+                                           void* y, void* stream) {
+    return guarded([&]() {
+        if (!matrix || matrix->kind != 0) invalid("spmv_device takes an undecorated matrix");
+        const BaseMatrix& A = *matrix->base;
+        const DirPlan& p = adjoint ? A.adj : A.mul;
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        static thread_local DevBuf zero_flag, partial;
+        if (!zero_flag.ptr) {
+            zero_flag.alloc(sizeof(int32_t));
+            CUDA_TRY(cudaMemset(zero_flag.ptr, 0, sizeof(int32_t)));
+        }
+        const size_t pbytes = (A.form == IRLBA_GB300_FORM_FP64 ? 8 : 4) * std::max<int64_t>(p.dev.npanels * p.dev.nrows, 1);
+        if (partial.bytes < pbytes) partial.alloc(pbytes);
+        if (A.form == IRLBA_GB300_FORM_FP64) {
+            Epilogue<double> e;
+            launch_spmv<double>(p.dev, static_cast<const double*>(x), static_cast<double*>(y), partial.as<double>(), e,
+                                zero_flag.as<int32_t>(), s);
+        } else {
+            Epilogue<float> e;
+            launch_spmv<float>(p.dev, static_cast<const float*>(x), static_cast<float*>(y), partial.as<float>(), e,
+                               zero_flag.as<int32_t>(), s);
+        }
+        CUDA_TRY(cudaGetLastError());
+    });
+}
+
+// Layout facts of a base matrix for byte accounting: nnz, stored value bytes,
+// index bytes (per direction), panels (per direction).
+irlba_gb300_status irlba_gb300_matrix_layout(const irlba_gb300_matrix* matrix, int64_t* nnz, int32_t* value_bytes,
+                                             int32_t* index_bytes_mul, int32_t* index_bytes_adj, int32_t* panels_mul,
+                                             int32_t* panels_adj) {
+    return guarded([&]() {
+        if (!matrix || matrix->kind != 0) invalid("matrix_layout takes an undecorated matrix");
+        const BaseMatrix& A = *matrix->base;
+        *nnz = A.mul.dev.nnz;
+        *value_bytes = A.store_f64 ? 8 : 4;
+        *index_bytes_mul = A.mul.dev.staged ? 2 : 4;
+        *index_bytes_adj = A.adj.dev.staged ? 2 : 4;
+        *panels_mul = A.mul.dev.npanels;
+        *panels_adj = A.adj.dev.npanels;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,155 @@
+// Kernel launchers of the GB300 IRLBA engine (host-callable, C++ linkage).
+#pragma once
+
+#include "common.cuh"
+
+namespace irlba_gb300 {
+
+// Threads per CTA of the SpMV kernels.
+constexpr int kSpmvThreads = 256;
+
+// One gather direction of a sparse operator, stored as a "panel CSR":
+// the input vector x (length ncols) is split into npanels column panels of
+// panel_width entries; segment (p, r) holds the entries of output row r whose
+// column falls in panel p, in panel-major order. Output
+//   y[r] = sum_p sum_{s in segment(p, r)} val[s] * x[p * panel_width + idx[s]].
+// staged = 1: the panel of x is copied to shared memory and idx16 holds the
+// column offset within the panel (u16). staged = 0: a single panel, x is
+// gathered from global memory, idx32 holds the column.
+struct DirPlanDev {
+    int64_t nrows = 0;
+    int64_t ncols = 0;
+    int64_t nnz = 0;
+    int32_t npanels = 1;
+    int32_t staged = 0;
+    int64_t panel_width = 0;
+    int64_t nseg = 0;
+    const int64_t* segptr = nullptr;   // nseg + 1
+    const uint16_t* idx16 = nullptr;
+    const int32_t* idx32 = nullptr;
+    const void* val = nullptr;
+    int32_t val_f64 = 0;
+    int32_t nblocks = 0;
+    const int64_t* block_seg = nullptr;  // nblocks + 1 segment boundaries per CTA
+    size_t smem_bytes = 0;
+};
+
+// Fused prologue/epilogue of a matvec (deferred centring and scaling, and the
+// Lanczos axpy). With acc the raw sparse product of row r:
+//   v = acc
+//   if (beta && !center_after) v -= *beta * (cvec ? cvec[r] : 1)
+//   if (oscale)               v = odivide ? v / oscale[r] : v * oscale[r]
+//   if (beta && center_after)  v -= *beta * (cvec ? cvec[r] : 1)
+//   if (alpha)                v -= *alpha * q[r]
+// The prologue scales x while staging: x'[c] = idivide ? x[c] / iscale[c] : x[c] * iscale[c].
+template <typename T>
+struct Epilogue {
+    const double* beta = nullptr;
+    const T* cvec = nullptr;
+    int32_t center_after = 0;
+    const T* oscale = nullptr;
+    int32_t odivide = 0;
+    const double* alpha = nullptr;
+    const T* q = nullptr;
+    const T* iscale = nullptr;
+    int32_t idivide = 0;
+};
+
+template <typename T>
+void launch_spmv(const DirPlanDev& p, const T* x, T* y, T* partial, const Epilogue<T>& e, const int32_t* abort,
+                 cudaStream_t stream);
+
+// Launch configuration helpers (dynamic shared-memory limits, occupancy, grids).
+cudaError_t spmv_configure(size_t max_smem);
+int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem);
+cudaError_t rotate_configure(size_t max_smem);
+int cgs_update_grid(int64_t L);
+int cgs_dot_grid(int64_t L);
+
+// out = prologue-scaled copy of x (used when x is not staged in shared memory).
+template <typename T>
+void launch_scale_vector(const T* x, const T* s, int32_t divide, int64_t n, T* out, cudaStream_t stream);
+
+// t[j] = sum_r Q[r, j] v[r] for j < c (FP64 accumulation); part: >= grid*c scratch.
+template <typename T>
+void launch_cgs_dot(const T* Q, int64_t L, int64_t ldq, int32_t c, const T* v, double* part, double* t, Ctrl* ctrl,
+                    cudaStream_t stream);
+
+// v -= Q[:, :c] t; then norm = ||v|| -> *norm_out (FP64); flags invariant if
+// check_eps and norm < ctrl->eps; null_start is raised instead when
+// check_null. When write_B >= 0, B[write_B] = *b_value (a device scalar) first.
+template <typename T>
+void launch_cgs_update(const T* Q, int64_t L, int64_t ldq, int32_t c, const double* t, T* v, double* part,
+                       double* norm_out, int32_t check_eps, int32_t check_null, Ctrl* ctrl, cudaStream_t stream);
+
+// v *= 1 / *norm; Q[:, col] = v (col >= 0); beta_out = sum f(v[i]) g[i] where
+// f applies the optional scale vector s (divide or multiply) and g is the
+// optional centre vector (NULL = 1). When bpos >= 0 also writes B[bpos] = S and
+// B[bpos + ldb] = R_F (the bidiagonal entries of the step).
+template <typename T>
+void launch_normalize(T* v, int64_t L, const double* norm, T* qcol, const T* fscale, int32_t fdivide,
+                      const T* gvec, double* beta_out, double* part, double* B, int64_t bpos, int64_t ldb,
+                      Ctrl* ctrl, cudaStream_t stream);
+
+// beta_out = sum f(x[i]) g[i] (no normalization).
+template <typename T>
+void launch_beta(const T* x, int64_t L, const T* fscale, int32_t fdivide, const T* gvec, double* beta_out,
+                 double* part, Ctrl* ctrl, cudaStream_t stream);
+
+// out[:, :k] = Q[:, :w] R[:, :k] row by row (in place allowed when out == Q);
+// R is FP64 column-major w x w (ld ldr). If fcol != NULL also sets
+// out[:, k] = fcol / *fnorm.
+template <typename T>
+void launch_rotate(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, T* out,
+                   int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream);
+
+// Same, writing FP64 output (the final U and V).
+template <typename T>
+void launch_rotate_out(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                       double* out, int64_t ldo, cudaStream_t stream);
+
+// Elementwise copy with conversion.
+template <typename A, typename B>
+void launch_convert(const A* in, B* out, int64_t n, cudaStream_t stream);
+
+// Dense column-major realization of one direction plan (rows x cols of the plan).
+void launch_realize(const DirPlanDev& p, double* out, int64_t ld, int32_t transpose, cudaStream_t stream);
+
+// Centre / scale applied to a realized column-major m x n matrix.
+void launch_realize_ops(double* A, int64_t m, int64_t n, const double* center, const double* scale,
+                        int32_t scale_column, int32_t scale_divide, int32_t center_outer, cudaStream_t stream);
+
+// Column sums and sums of squared deviations of the matrix whose gather plan
+// over features is `p` (rows of p = features): mean[f] = sum / nobs,
+// var[f] = (sum (x - mean)^2 + (nobs - nnz_f) mean^2) / (nobs - 1).
+void launch_feature_stats(const DirPlanDev& p, int64_t nobs, int32_t center, int32_t scale, double* center_out,
+                          double* scale_out, double* scratch, cudaStream_t stream);
+
+// Restart of the IRLBA loop on the device (compute.hpp:225-293): SVD of B,
+// convergence test, update_k, and B rebuilt for the next Lanczos run.
+struct RestartArgs {
+    double* B;          // work x work, column-major
+    double* BS;         // work
+    double* BU;         // work x work
+    double* BV;         // work x work
+    double* prevS;      // work
+    double* res;        // work
+    double* scratch;    // >= 2 * work * work doubles when the SVD does not fit in shared memory
+    int32_t work;
+    int32_t k;          // start column of the run that produced B
+    int32_t requested;
+    int32_t iter;
+    double tol;
+    double svtol;
+    Ctrl* ctrl;
+};
+void launch_restart(const RestartArgs& a, cudaStream_t stream, size_t max_smem);
+size_t restart_smem_bytes(int work);
+cudaError_t restart_configure(size_t max_smem);
+
+// Thin SVD of a dense column-major m x n matrix with m >= n (one-sided Jacobi):
+// U m x n, S n (descending), V n x n. scratch >= m*n + n*n doubles.
+void launch_dense_svd(const double* A, int64_t m, int64_t n, double* U, double* S, double* V, double* scratch,
+                      Ctrl* ctrl, cudaStream_t stream);
+
+}  // namespace irlba_gb300

@@ -1,0 +1,459 @@
+// Tall-skinny kernels of the IRLBA loop:
+//  * classical Gram-Schmidt reorthogonalization, orthogonalize_vector in
+//    CppIrlba's lanczos.hpp:17-21 (t = Q^T v; v -= Q t), as two passes over Q:
+//    a GEMV-transpose with per-CTA partials reduced by the last CTA in a fixed
+//    order, then the GEMV update fused with the norm of the result;
+//  * normalization of a Lanczos vector fused with the centring scalar of the
+//    next matvec and the bidiagonal entries (lanczos.hpp:85-86,108-113,131-134);
+//  * the restart rotations V <- V BV, W <- W BU (compute.hpp:268-280) and the
+//    output assembly (compute.hpp:298-305);
+//  * realization and PCA column statistics (pca.hpp:85-109).
+// Coefficients and norms accumulate in FP64 in both precision forms: in the FP32
+// form each lane sums 8 FP32 products before adding them to an FP64 total.
+
+#include "kernels.cuh"
+
+namespace irlba_gb300 {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kDotRows = 4096;     // rows per CTA of the GEMV-transpose pass
+constexpr int kMaxCols = 1024;     // basis columns held in shared memory
+
+int grid_for(int64_t n, int threads, int cap) {
+    int64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return static_cast<int>(g);
+}
+
+// ---------------------------------------------------------------------------
+// t = Q[:, :c]^T v
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cgs_dot_kernel(const T* __restrict__ Q, int64_t L, int64_t ldq, int32_t c,
+                                                           const T* __restrict__ v, double* __restrict__ part,
+                                                           double* __restrict__ t, Ctrl* ctrl) {
+    __shared__ T vs[kDotRows];
+    __shared__ bool is_last;
+    if (ctrl->abort) return;
+    const int64_t r0 = static_cast<int64_t>(blockIdx.x) * kDotRows;
+    const int rows = static_cast<int>((L - r0 < kDotRows ? L - r0 : static_cast<int64_t>(kDotRows)));
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) vs[i] = v[r0 + i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < c; j += nw) {
+        const T* __restrict__ q = Q + j * ldq + r0;
+        double acc = 0;
+        int i = lane;
+        for (; i + 7 * 32 < rows; i += 8 * 32) {
+            T s = 0;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += q[i + u * 32] * vs[i + u * 32];
+            acc += static_cast<double>(s);
+        }
+        {
+            T s = 0;
+            for (; i < rows; i += 32) s += q[i] * vs[i];
+            acc += static_cast<double>(s);
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) part[static_cast<int64_t>(blockIdx.x) * c + j] = acc;
+    }
+
+    if (last_block(&ctrl->ticket[kTicketDot], &is_last)) {
+        for (int j = threadIdx.x; j < c; j += blockDim.x) {
+            double s = 0;
+            for (int b = 0; b < static_cast<int>(gridDim.x); ++b) s += __ldcg(part + static_cast<int64_t>(b) * c + j);
+            t[j] = s;
+        }
+        if (threadIdx.x == 0) ctrl->ticket[kTicketDot] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// v -= Q[:, :c] t ; norm = ||v||
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cgs_update_kernel(const T* __restrict__ Q, int64_t L, int64_t ldq,
+                                                              int32_t c, const double* __restrict__ t,
+                                                              T* __restrict__ v, double* __restrict__ part,
+                                                              double* norm_out, int32_t check_eps, int32_t check_null,
+                                                              Ctrl* ctrl) {
+    __shared__ T ts[kMaxCols];
+    __shared__ double red[32];
+    __shared__ bool is_last;
+    if (ctrl->abort) return;
+    for (int j = threadIdx.x; j < c; j += blockDim.x) ts[j] = static_cast<T>(t[j]);
+    __syncthreads();
+
+    double sq = 0;
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < L;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        T s = 0;
+        const T* __restrict__ q = Q + r;
+        int j = 0;
+        for (; j + 3 < c; j += 4) {
+            const T q0 = q[j * ldq], q1 = q[(j + 1) * ldq], q2 = q[(j + 2) * ldq], q3 = q[(j + 3) * ldq];
+            s += q0 * ts[j];
+            s += q1 * ts[j + 1];
+            s += q2 * ts[j + 2];
+            s += q3 * ts[j + 3];
+        }
+        for (; j < c; ++j) s += q[j * ldq] * ts[j];
+        const T nv = v[r] - s;
+        v[r] = nv;
+        sq += static_cast<double>(nv) * static_cast<double>(nv);
+    }
+    const double bs = block_sum(sq, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = bs;
+
+    if (last_block(&ctrl->ticket[kTicketUpdate], &is_last)) {
+        if (threadIdx.x == 0) {
+            double s = 0;
+            for (int b = 0; b < static_cast<int>(gridDim.x); ++b) s += __ldcg(part + b);
+            const double nrm = sqrt(s);
+            *norm_out = nrm;
+            if (check_null && nrm < ctrl->eps) {
+                ctrl->null_start = 1;
+                ctrl->abort = 1;
+            } else if (check_eps && nrm < ctrl->eps) {
+                ctrl->invariant = 1;
+                ctrl->abort = 1;
+            }
+            ctrl->ticket[kTicketUpdate] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// v /= norm; qcol = v; beta = sum f(v) g; B entries.
+// ---------------------------------------------------------------------------
+template <typename T, bool NORMALIZE>
+__global__ void __launch_bounds__(kThreads) normalize_kernel(T* __restrict__ v, int64_t L, const double* norm,
+                                                             T* __restrict__ qcol, const T* __restrict__ fscale,
+                                                             int32_t fdivide, const T* __restrict__ gvec,
+                                                             double* beta_out, double* __restrict__ part, double* B,
+                                                             int64_t bpos, int64_t ldb, Ctrl* ctrl) {
+    __shared__ double red[32];
+    __shared__ bool is_last;
+    if (ctrl->abort) return;
+    T inv = 1;
+    if (NORMALIZE) inv = static_cast<T>(1.0 / *norm);
+    double acc = 0;
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < L;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        T x = v[r];
+        if (NORMALIZE) {
+            x = x * inv;
+            v[r] = x;
+            if (qcol) qcol[r] = x;
+        }
+        if (beta_out) {
+            T f = x;
+            if (fscale) f = fdivide ? f / fscale[r] : f * fscale[r];
+            if (gvec) acc += static_cast<double>(f * gvec[r]);
+            else acc += static_cast<double>(f);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && B && bpos >= 0) {
+        B[bpos] = ctrl->S;
+        B[bpos + ldb] = ctrl->R_F;
+    }
+    if (!beta_out) return;
+    const double bs = block_sum(acc, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = bs;
+    if (last_block(&ctrl->ticket[kTicketNormalize], &is_last)) {
+        if (threadIdx.x == 0) {
+            double s = 0;
+            for (int b = 0; b < static_cast<int>(gridDim.x); ++b) s += __ldcg(part + b);
+            *beta_out = s;
+            ctrl->ticket[kTicketNormalize] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// out[:, :k] = Q[:, :w] R[:, :k] (+ out[:, k] = fcol / fnorm)
+// ---------------------------------------------------------------------------
+template <typename T, typename O, int WMAX>
+__global__ void __launch_bounds__(128) rotate_kernel(const T* Q, int64_t L, int64_t ldq, int32_t w,
+                                                     const double* __restrict__ R, int32_t ldr, int32_t k, O* out,
+                                                     int64_t ldo, const T* __restrict__ fcol,
+                                                     const double* fnorm, const int32_t* abort) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    // Rs[j * k + i] = R[j, i] for j < w, zero for w <= j < WMAX.
+    T* Rs = reinterpret_cast<T*>(smem_raw);
+    if (abort && *abort) return;
+    for (int idx = threadIdx.x; idx < WMAX * k; idx += blockDim.x) {
+        const int j = idx / k, i = idx % k;
+        Rs[idx] = j < w ? static_cast<T>(R[j + static_cast<int64_t>(i) * ldr]) : T(0);
+    }
+    __syncthreads();
+    T finv = 0;
+    if (fcol) finv = static_cast<T>(1.0 / *fnorm);
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < L;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        T row[WMAX];
+#pragma unroll
+        for (int j = 0; j < WMAX; ++j) row[j] = (j < w) ? Q[r + j * ldq] : T(0);
+        for (int i = 0; i < k; ++i) {
+            T s = 0;
+#pragma unroll
+            for (int j = 0; j < WMAX; ++j) s += row[j] * Rs[j * k + i];
+            out[r + i * ldo] = static_cast<O>(s);
+        }
+        if (fcol) out[r + static_cast<int64_t>(k) * ldo] = static_cast<O>(fcol[r] * finv);
+    }
+}
+
+template <typename T, typename O>
+void rotate_dispatch(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, O* out,
+                     int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream) {
+    const int grid = grid_for(L, 128, 152 * 8);
+    const int kk = k > 0 ? k : 1;
+    if (w <= 16) {
+        rotate_kernel<T, O, 16><<<grid, 128, sizeof(T) * 16 * kk, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort); count_launch();
+    } else if (w <= 32) {
+        rotate_kernel<T, O, 32><<<grid, 128, sizeof(T) * 32 * kk, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort); count_launch();
+    } else if (w <= 64) {
+        rotate_kernel<T, O, 64><<<grid, 128, sizeof(T) * 64 * kk, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort); count_launch();
+    } else {
+        rotate_kernel<T, O, 128><<<grid, 128, sizeof(T) * 128 * kk, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort); count_launch();
+    }
+}
+
+template <typename A, typename B>
+__global__ void convert_kernel(const A* __restrict__ in, B* __restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = static_cast<B>(in[i]);
+}
+
+// Scatter of a direction plan into a dense column-major matrix. The plan's rows
+// are matrix rows (transpose = 0) or matrix columns (transpose = 1).
+template <typename VT>
+__global__ void realize_kernel(const DirPlanDev p, double* out, int64_t ld, int32_t transpose) {
+    const VT* val = static_cast<const VT*>(p.val);
+    for (int64_t seg = blockIdx.x; seg < p.nseg; seg += gridDim.x) {
+        const int64_t panel = seg / p.nrows, row = seg % p.nrows;
+        for (int64_t s = p.segptr[seg] + threadIdx.x; s < p.segptr[seg + 1]; s += blockDim.x) {
+            const int64_t col = p.staged ? panel * p.panel_width + p.idx16[s] : p.idx32[s];
+            const double v = static_cast<double>(val[s]);
+            if (transpose) out[row * ld + col] = v;
+            else out[col * ld + row] = v;
+        }
+    }
+}
+
+__global__ void realize_ops_kernel(double* A, int64_t m, int64_t n, const double* center, const double* scale,
+                                   int32_t scale_column, int32_t scale_divide, int32_t center_outer) {
+    const int64_t total = m * n;
+    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = e % m, c = e / m;
+        double v = A[e];
+        if (center && !center_outer) v -= center[c];
+        if (scale) {
+            const double s = scale_column ? scale[c] : scale[r];
+            v = scale_divide ? v / s : v * s;
+        }
+        if (center && center_outer) v -= center[c];
+        A[e] = v;
+    }
+}
+
+// Per-feature sums over segments of a plan whose rows are features.
+template <typename VT>
+__global__ void feature_sums_kernel(const DirPlanDev p, const double* mean, double* out_sum, double* out_cnt) {
+    const VT* val = static_cast<const VT*>(p.val);
+    __shared__ double red[32];
+    for (int64_t f = blockIdx.x; f < p.nrows; f += gridDim.x) {
+        double acc = 0, cnt = 0;
+        for (int32_t pnl = 0; pnl < p.npanels; ++pnl) {
+            const int64_t seg = pnl * p.nrows + f;
+            const int64_t b = p.segptr[seg], en = p.segptr[seg + 1];
+            if (threadIdx.x == 0) cnt += static_cast<double>(en - b);
+            for (int64_t s = b + threadIdx.x; s < en; s += blockDim.x) {
+                const double x = static_cast<double>(val[s]);
+                if (mean) {
+                    const double d = x - mean[f];
+                    acc += d * d;
+                } else {
+                    acc += x;
+                }
+            }
+        }
+        const double tot = block_sum(acc, red);
+        if (threadIdx.x == 0) {
+            out_sum[f] = tot;
+            if (out_cnt) out_cnt[f] = cnt;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void feature_finalize_kernel(int64_t nf, int64_t nobs, int32_t center, int32_t scale, const double* sum,
+                                        const double* cnt, const double* ssd, double* center_out, double* scale_out,
+                                        double* mean_tmp, int32_t stage) {
+    for (int64_t f = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; f < nf;
+         f += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (stage == 0) {
+            const double mean = center ? sum[f] / static_cast<double>(nobs) : 0.0;
+            mean_tmp[f] = mean;
+            if (center) center_out[f] = mean;
+        } else {
+            const double mean = mean_tmp[f];
+            const double var = ssd[f] + (static_cast<double>(nobs) - cnt[f]) * mean * mean;
+            scale_out[f] = var != 0 ? sqrt(var / static_cast<double>(nobs - 1)) : 1.0;
+        }
+    }
+}
+
+}  // namespace
+
+template <typename T>
+void launch_cgs_dot(const T* Q, int64_t L, int64_t ldq, int32_t c, const T* v, double* part, double* t, Ctrl* ctrl,
+                    cudaStream_t stream) {
+    if (c <= 0 || L == 0) return;
+    const int grid = static_cast<int>((L + kDotRows - 1) / kDotRows);
+    cgs_dot_kernel<T><<<grid, kThreads, 0, stream>>>(Q, L, ldq, c, v, part, t, ctrl); count_launch();
+}
+
+int cgs_update_grid(int64_t L) { return grid_for(L, kThreads, 152 * 8); }
+int cgs_dot_grid(int64_t L) { return static_cast<int>((L + kDotRows - 1) / kDotRows); }
+
+template <typename T>
+void launch_cgs_update(const T* Q, int64_t L, int64_t ldq, int32_t c, const double* t, T* v, double* part,
+                       double* norm_out, int32_t check_eps, int32_t check_null, Ctrl* ctrl, cudaStream_t stream) {
+    cgs_update_kernel<T><<<cgs_update_grid(L), kThreads, 0, stream>>>(Q, L, ldq, c, t, v, part, norm_out, check_eps,
+                                                                     check_null, ctrl); count_launch();
+}
+
+template <typename T>
+void launch_normalize(T* v, int64_t L, const double* norm, T* qcol, const T* fscale, int32_t fdivide, const T* gvec,
+                      double* beta_out, double* part, double* B, int64_t bpos, int64_t ldb, Ctrl* ctrl,
+                      cudaStream_t stream) {
+    normalize_kernel<T, true><<<cgs_update_grid(L), kThreads, 0, stream>>>(v, L, norm, qcol, fscale, fdivide, gvec,
+                                                                          beta_out, part, B, bpos, ldb, ctrl); count_launch();
+}
+
+template <typename T>
+void launch_beta(const T* x, int64_t L, const T* fscale, int32_t fdivide, const T* gvec, double* beta_out,
+                 double* part, Ctrl* ctrl, cudaStream_t stream) {
+    normalize_kernel<T, false><<<cgs_update_grid(L), kThreads, 0, stream>>>(const_cast<T*>(x), L, nullptr, nullptr,
+                                                                           fscale, fdivide, gvec, beta_out, part,
+                                                                           nullptr, -1, 0, ctrl); count_launch();
+}
+
+template <typename T>
+void launch_rotate(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, T* out,
+                   int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream) {
+    if (L == 0 || (k == 0 && !fcol)) return;
+    rotate_dispatch<T, T>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, stream);
+}
+
+template <typename T>
+void launch_rotate_out(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                       double* out, int64_t ldo, cudaStream_t stream) {
+    if (L == 0 || k == 0) return;
+    rotate_dispatch<T, double>(Q, L, ldq, w, R, ldr, k, out, ldo, static_cast<const T*>(nullptr), nullptr, nullptr,
+                               stream);
+}
+
+template <typename T, typename O>
+cudaError_t rotate_configure_one(size_t max_smem) {
+    const int b = static_cast<int>(max_smem);
+    cudaError_t e = cudaFuncSetAttribute(rotate_kernel<T, O, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(rotate_kernel<T, O, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(rotate_kernel<T, O, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(rotate_kernel<T, O, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    return e;
+}
+
+cudaError_t rotate_configure(size_t max_smem) {
+    cudaError_t e = rotate_configure_one<float, float>(max_smem);
+    if (e == cudaSuccess) e = rotate_configure_one<double, double>(max_smem);
+    if (e == cudaSuccess) e = rotate_configure_one<float, double>(max_smem);
+    return e;
+}
+
+template <typename A, typename B>
+void launch_convert(const A* in, B* out, int64_t n, cudaStream_t stream) {
+    if (n == 0) return;
+    convert_kernel<A, B><<<grid_for(n, 256, 152 * 16), 256, 0, stream>>>(in, out, n); count_launch();
+}
+
+void launch_realize(const DirPlanDev& p, double* out, int64_t ld, int32_t transpose, cudaStream_t stream) {
+    if (p.nseg == 0) return;
+    const int grid = static_cast<int>(std::min<int64_t>(p.nseg, 152 * 64));
+    if (p.val_f64) {
+        realize_kernel<double><<<grid, 128, 0, stream>>>(p, out, ld, transpose);
+    } else {
+        realize_kernel<float><<<grid, 128, 0, stream>>>(p, out, ld, transpose);
+    }
+    count_launch();
+}
+
+void launch_realize_ops(double* A, int64_t m, int64_t n, const double* center, const double* scale,
+                        int32_t scale_column, int32_t scale_divide, int32_t center_outer, cudaStream_t stream) {
+    if (m * n == 0) return;
+    realize_ops_kernel<<<grid_for(m * n, 256, 152 * 16), 256, 0, stream>>>(A, m, n, center, scale, scale_column,
+                                                                         scale_divide, center_outer); count_launch();
+}
+
+// scratch: 4 * nrows doubles.
+void launch_feature_stats(const DirPlanDev& p, int64_t nobs, int32_t center, int32_t scale, double* center_out,
+                          double* scale_out, double* scratch, cudaStream_t stream) {
+    const int64_t nf = p.nrows;
+    if (nf == 0) return;
+    double* sum = scratch;
+    double* cnt = scratch + nf;
+    double* ssd = scratch + 2 * nf;
+    double* mean = scratch + 3 * nf;
+    const int grid = static_cast<int>(std::min<int64_t>(nf, 152 * 16));
+    if (p.val_f64) {
+        feature_sums_kernel<double><<<grid, 256, 0, stream>>>(p, nullptr, sum, cnt);
+    } else {
+        feature_sums_kernel<float><<<grid, 256, 0, stream>>>(p, nullptr, sum, cnt);
+    }
+    count_launch();
+    feature_finalize_kernel<<<grid_for(nf, 256, 1024), 256, 0, stream>>>(nf, nobs, center, scale, sum, cnt, ssd,
+                                                                         center_out, scale_out, mean, 0); count_launch();
+    if (scale) {
+        if (p.val_f64) {
+            feature_sums_kernel<double><<<grid, 256, 0, stream>>>(p, mean, ssd, nullptr);
+        } else {
+            feature_sums_kernel<float><<<grid, 256, 0, stream>>>(p, mean, ssd, nullptr);
+        }
+        count_launch();
+        feature_finalize_kernel<<<grid_for(nf, 256, 1024), 256, 0, stream>>>(nf, nobs, center, scale, sum, cnt, ssd,
+                                                                             center_out, scale_out, mean, 1); count_launch();
+    }
+}
+
+#define IRLBA_INST(T)                                                                                               \
+    template void launch_cgs_dot<T>(const T*, int64_t, int64_t, int32_t, const T*, double*, double*, Ctrl*,         \
+                                    cudaStream_t);                                                                  \
+    template void launch_cgs_update<T>(const T*, int64_t, int64_t, int32_t, const double*, T*, double*, double*,   \
+                                       int32_t, int32_t, Ctrl*, cudaStream_t);                                      \
+    template void launch_normalize<T>(T*, int64_t, const double*, T*, const T*, int32_t, const T*, double*,         \
+                                      double*, double*, int64_t, int64_t, Ctrl*, cudaStream_t);                     \
+    template void launch_beta<T>(const T*, int64_t, const T*, int32_t, const T*, double*, double*, Ctrl*,           \
+                                 cudaStream_t);                                                                     \
+    template void launch_rotate<T>(const T*, int64_t, int64_t, int32_t, const double*, int32_t, int32_t, T*,        \
+                                   int64_t, const T*, const double*, const int32_t*, cudaStream_t);                 \
+    template void launch_rotate_out<T>(const T*, int64_t, int64_t, int32_t, const double*, int32_t, int32_t,       \
+                                       double*, int64_t, cudaStream_t);
+IRLBA_INST(float)
+IRLBA_INST(double)
+#undef IRLBA_INST
+
+template void launch_convert<float, double>(const float*, double*, int64_t, cudaStream_t);
+template void launch_convert<double, float>(const double*, float*, int64_t, cudaStream_t);
+template void launch_convert<double, double>(const double*, double*, int64_t, cudaStream_t);
+template void launch_convert<float, float>(const float*, float*, int64_t, cudaStream_t);
+
+}  // namespace irlba_gb300

@@ -1,0 +1,204 @@
+/*
+ * irlba_gb300.h — C ABI of the GB300 (sm_103a) IRLBA engine.
+ *
+ * This is the only entry into the CUDA engine. Every function returns an
+ * irlba_gb300_status; on failure, irlba_gb300_last_error() gives a message whose
+ * wording follows the exception text CppIrlba throws for the same condition.
+ * Plain pointers and sizes only. Host pointers unless a name says "device".
+ *
+ * Reference interfaces replaced (CppIrlba, paths relative to its project root):
+ *   matrix handles      <- irlba::Matrix and subclasses   include/irlba/Matrix/interface.hpp:141-223
+ *   sparse create       <- irlba::ParallelSparseMatrix    include/irlba/Matrix/sparse.hpp:469-471
+ *   dense create        <- irlba::SimpleMatrix            include/irlba/Matrix/simple.hpp:124-178
+ *   center              <- irlba::CenteredMatrix          include/irlba/Matrix/centered.hpp:139-204
+ *   scale               <- irlba::ScaledMatrix            include/irlba/Matrix/scaled.hpp:195-268
+ *   multiply            <- Workspace::multiply            include/irlba/Matrix/interface.hpp:49
+ *   adjoint_multiply    <- AdjointWorkspace::multiply     include/irlba/Matrix/interface.hpp:87
+ *   realize             <- RealizeWorkspace::realize_copy include/irlba/Matrix/interface.hpp:125-130
+ *   options             <- irlba::Options                 include/irlba/Options.hpp:19-83
+ *   compute             <- irlba::compute                 include/irlba/compute.hpp:141-308
+ *   pca                 <- irlba::pca                     include/irlba/pca.hpp:55-139
+ *   orthogonalize       <- irlba::orthogonalize_vector    include/irlba/lanczos.hpp:17-21
+ */
+#ifndef IRLBA_GB300_H
+#define IRLBA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    IRLBA_GB300_OK = 0,
+    IRLBA_GB300_ERROR_INVALID_ARGUMENT = 1, /* messages as the reference's std::runtime_error */
+    IRLBA_GB300_ERROR_CUDA = 2,             /* a CUDA call failed (no GPU, out of memory, ...) */
+    IRLBA_GB300_ERROR_NUMERICAL = 3,        /* e.g. starting vector near the null space */
+    IRLBA_GB300_ERROR_UNSUPPORTED = 4       /* a decorator chain the engine does not fuse */
+} irlba_gb300_status;
+
+typedef enum {
+    IRLBA_GB300_VALUE_F32 = 0,
+    IRLBA_GB300_VALUE_F64 = 1
+} irlba_gb300_value_type;
+
+/* Arithmetic form of the Lanczos loop. */
+typedef enum {
+    /* FP64 matrix values, basis, matvecs, recurrence and restart (matches the reference). */
+    IRLBA_GB300_FORM_FP64 = 0,
+    /* FP32 matrix values, basis and matvecs with FP32 accumulation; FP64 for the
+     * reorthogonalization coefficients and norms, the bidiagonal recurrence
+     * (alpha/beta), the restart small SVD and the residual convergence test. */
+    IRLBA_GB300_FORM_FP32_FP64STEPS = 1
+} irlba_gb300_form;
+
+/* Mirrors irlba::Options (Options.hpp:19-83); same names, meanings and defaults.
+ * `initial` is the optional start vector (length = columns of the matrix), or NULL. */
+typedef struct {
+    double invariant_subspace_tolerance;   /* -1 -> eps^0.8 */
+    double convergence_tolerance;          /* 1e-5 */
+    double singular_value_ratio_tolerance; /* -1 -> convergence_tolerance */
+    int32_t extra_work;                    /* 7 */
+    int32_t max_iterations;                /* 1000 */
+    int32_t exact_for_small_matrix;        /* 1 */
+    int32_t exact_for_large_number;        /* 1 */
+    int32_t cap_number;                    /* 0 */
+    int32_t reserved0;
+    uint64_t seed;                         /* std::mt19937_64::default_seed = 5489 */
+    const double* initial;                 /* NULL = random normals from `seed` */
+    int64_t initial_size;
+} irlba_gb300_options;
+
+/* Per-call statistics (not part of the reference's Results). */
+typedef struct {
+    int64_t matvecs;          /* multiply + adjoint_multiply calls */
+    int64_t lanczos_steps;
+    int64_t restarts;
+    int64_t careful_restarts; /* restarts re-run to refill an invariant subspace */
+    double seconds_total;     /* host wall time of the call */
+    double device_ms;         /* CUDA-event time of the call on its stream */
+    int64_t kernel_launches;  /* kernels this library launched during the call */
+} irlba_gb300_stats;
+
+/* Opaque matrix handle: a base matrix or a centre/scale decorator over one. */
+typedef struct irlba_gb300_matrix irlba_gb300_matrix;
+
+void irlba_gb300_default_options(irlba_gb300_options* options);
+const char* irlba_gb300_last_error(void);
+/* Number of CUDA devices visible, or -1 if the runtime cannot be queried. */
+int irlba_gb300_device_count(void);
+
+/* ParallelSparseMatrix(nrow, ncol, x, i, p, column_major, num_threads) (sparse.hpp:469).
+ * values: nnz entries of value_type; indices: int32 row (column_major) or column
+ * indices, sorted within each primary element; pointers: int64, length primary+1.
+ * The data are copied to the device. `form` fixes the stored value precision. */
+irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, const void* values,
+                                                    irlba_gb300_value_type value_type, const int32_t* indices,
+                                                    const int64_t* pointers, int32_t column_major,
+                                                    irlba_gb300_form form, irlba_gb300_matrix** out);
+
+/* SimpleMatrix over a dense matrix (simple.hpp:124-178); column-major unless
+ * row_major != 0; `ld` is the leading dimension. Copied to the device. */
+irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, const void* values,
+                                                   irlba_gb300_value_type value_type, int64_t ld,
+                                                   int32_t row_major, irlba_gb300_form form,
+                                                   irlba_gb300_matrix** out);
+
+/* CenteredMatrix(inner, center) (centered.hpp:152): column centring, center has
+ * length ncol. The inner handle must outlive the new one. */
+irlba_gb300_status irlba_gb300_matrix_center(const irlba_gb300_matrix* inner, const double* center,
+                                             irlba_gb300_matrix** out);
+
+/* ScaledMatrix(inner, scale, column, divide) (scaled.hpp:420). scale has length
+ * ncol (column != 0) or nrow. The inner handle must outlive the new one. */
+irlba_gb300_status irlba_gb300_matrix_scale(const irlba_gb300_matrix* inner, const double* scale, int32_t column,
+                                            int32_t divide, irlba_gb300_matrix** out);
+
+irlba_gb300_status irlba_gb300_matrix_destroy(irlba_gb300_matrix* matrix);
+irlba_gb300_status irlba_gb300_matrix_dims(const irlba_gb300_matrix* matrix, int64_t* nrow, int64_t* ncol);
+
+/* Workspace::multiply: output (length nrow) = A * right (length ncol). The output
+ * is fully overwritten, whatever it held. Host buffers. */
+irlba_gb300_status irlba_gb300_multiply(const irlba_gb300_matrix* matrix, const double* right, double* output);
+/* AdjointWorkspace::multiply: output (length ncol) = A^T * right (length nrow). */
+irlba_gb300_status irlba_gb300_adjoint_multiply(const irlba_gb300_matrix* matrix, const double* right,
+                                                double* output);
+/* RealizeWorkspace::realize_copy: column-major nrow x ncol dense copy. */
+irlba_gb300_status irlba_gb300_realize(const irlba_gb300_matrix* matrix, double* output);
+
+/* irlba::compute(matrix, number, outU, outV, outD, options) (compute.hpp:141-308).
+ * U: nrow x number, V: ncol x number (column-major), D: number. If cap_number
+ * lowers `number`, *out_number says how many were written. Returns converged and
+ * the restart iteration count as the reference's std::pair. */
+irlba_gb300_status irlba_gb300_compute(const irlba_gb300_matrix* matrix, int64_t number,
+                                       const irlba_gb300_options* options, double* U, double* V, double* D,
+                                       int64_t* out_number, int32_t* converged, int32_t* iterations,
+                                       irlba_gb300_stats* stats);
+
+/* irlba::pca(matrix, center, scale, number, scores, rotation, variances, options)
+ * (pca.hpp:55-139) on a base (undecorated) matrix whose rows are observations.
+ * Column means and standard deviations are computed on the device; centring and
+ * scaling are deferred into the matvecs. scores: nrow x number; rotation:
+ * ncol x number; variances: number. center_out / scale_out (length ncol) may be
+ * NULL. */
+irlba_gb300_status irlba_gb300_pca(const irlba_gb300_matrix* matrix, int32_t center, int32_t scale, int64_t number,
+                                   const irlba_gb300_options* options, double* scores, double* rotation,
+                                   double* variances, int64_t* out_number, int32_t* converged, int32_t* iterations,
+                                   double* center_out, double* scale_out, irlba_gb300_stats* stats);
+
+/* orthogonalize_vector(mat, vec, ncols, tmp) (lanczos.hpp:17-21) on device memory:
+ * vec -= Q[:, :ncols] (Q[:, :ncols]^T vec), Q column-major L x ldq-strided,
+ * FP64. `stream` is a cudaStream_t (NULL = legacy default stream). Scratch for
+ * the partial dot products is allocated by the library per call. */
+irlba_gb300_status irlba_gb300_orthogonalize_vector_device(const double* Q, int64_t L, int64_t ldq, int64_t ncols,
+                                                           double* vec, void* stream);
+
+/* ---- Extensions without a counterpart in the reference --------------------- */
+
+/* irlba_gb300_compute with U (nrow x number), V (ncol x number) and D (number)
+ * in device memory, issued on `stream` (a cudaStream_t; NULL = an internal
+ * stream). The call returns when the results are complete. */
+irlba_gb300_status irlba_gb300_compute_device(const irlba_gb300_matrix* matrix, int64_t number,
+                                              const irlba_gb300_options* options, double* U_device,
+                                              double* V_device, double* D_device, int64_t* out_number,
+                                              int32_t* converged, int32_t* iterations, irlba_gb300_stats* stats,
+                                              void* stream);
+
+/* irlba_gb300_pca with scores (nrow x number), rotation (ncol x number) and
+ * variances (number) in device memory, issued on `stream` (NULL = internal). */
+irlba_gb300_status irlba_gb300_pca_device(const irlba_gb300_matrix* matrix, int32_t center, int32_t scale,
+                                          int64_t number, const irlba_gb300_options* options, double* scores_device,
+                                          double* rotation_device, double* variances_device, int64_t* out_number,
+                                          int32_t* converged, int32_t* iterations, irlba_gb300_stats* stats,
+                                          void* stream);
+
+/* One direction of the raw sparse product of an undecorated matrix on device
+ * vectors: y = A x (adjoint = 0) or y = A^T x. Vectors are FP64 for FP64-form
+ * matrices and FP32 for the FP32 form. Asynchronous on `stream`. */
+irlba_gb300_status irlba_gb300_spmv_device(const irlba_gb300_matrix* matrix, int32_t adjoint, const void* x,
+                                           void* y, void* stream);
+
+/* Stored layout of an undecorated matrix, for byte accounting. */
+irlba_gb300_status irlba_gb300_matrix_layout(const irlba_gb300_matrix* matrix, int64_t* nnz, int32_t* value_bytes,
+                                             int32_t* index_bytes_mul, int32_t* index_bytes_adj,
+                                             int32_t* panels_mul, int32_t* panels_adj);
+
+/* Per-kernel-class CUDA-event timing of compute calls, off by default.
+ * Classes: 0 SpMV multiply, 1 SpMV adjoint, 2 reorthogonalization,
+ * 3 restart (small SVD), 4 rotation, 5 other. */
+void irlba_gb300_set_profiling(int32_t on);
+void irlba_gb300_last_profile(double* ms, int64_t* launches);
+
+/* Kernels launched by this library since the process started. */
+int64_t irlba_gb300_launch_count(void);
+
+/* Bytes this library copied host-to-device and device-to-host since the
+ * process started (either pointer may be NULL). */
+void irlba_gb300_transfer_bytes(int64_t* h2d, int64_t* d2h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IRLBA_GB300_H */

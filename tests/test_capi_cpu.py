@@ -1,0 +1,71 @@
+"""C ABI checks that need no GPU: the library builds and loads, exports every
+function include/*.h declares, and refuses to compute without a device."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cppirlba_gb300 as eng
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(irlba_gb300_\w+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_library_exports_all_declared_symbols():
+    lib = ctypes.CDLL(eng.library_path())
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_default_options_match_reference():
+    o = eng._Options()
+    eng.load_library().irlba_gb300_default_options(ctypes.byref(o))
+    d = eng.Options()
+    # Options.hpp:31-80 defaults
+    assert o.invariant_subspace_tolerance == d.invariant_subspace_tolerance == -1
+    assert o.convergence_tolerance == d.convergence_tolerance == 1e-5
+    assert o.singular_value_ratio_tolerance == -1
+    assert o.extra_work == 7 and o.max_iterations == 1000
+    assert o.exact_for_small_matrix == 1 and o.exact_for_large_number == 1 and o.cap_number == 0
+    assert o.seed == d.seed == 5489
+
+
+def test_fails_loudly_without_gpu():
+    if eng.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(eng.IrlbaError) as e:
+        eng.SimpleMatrix(np.eye(4))
+    assert e.value.status == eng.ERROR_CUDA
+
+
+def test_datagen_deterministic_and_dense_enough():
+    from cppirlba_gb300 import datagen
+    a = datagen.scrna_gene_major(50, 4000, 0.1, seed=11)
+    b = datagen.scrna_gene_major(50, 4000, 0.1, seed=11)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    ptr, idx, val = a
+    dens = ptr[-1] / (50 * 4000)
+    assert 0.09 < dens < 0.11
+    assert np.all(val >= np.log1p(1.0) - 1e-6)
+    for g in range(50):
+        seg = idx[ptr[g]:ptr[g + 1]]
+        assert np.all(np.diff(seg) > 0) and (seg.size == 0 or (seg[0] >= 0 and seg[-1] < 4000))
+    tp, ti, tv = datagen.transpose_compressed(50, 4000, ptr, idx, val)
+    inp = datagen.SparseInput(4000, 50, ptr, idx, val, column_major=True)
+    inp2 = datagen.SparseInput(4000, 50, tp, ti, tv, column_major=False)
+    np.testing.assert_array_equal(inp.to_dense(), inp2.to_dense())
