@@ -37,6 +37,14 @@ TOL = 1e-5
 REFERENCE_STEPS_TO_TOL = None
 
 
+T_START = time.time()
+
+
+def log(msg):
+    """Progress to stderr (the JSON line alone goes to stdout)."""
+    print("[bench %7.1fs] %s" % (time.time() - T_START, msg), file=sys.stderr, flush=True)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -206,6 +214,7 @@ def main():
     t_gen = time.perf_counter()
     inp = make_input(args)
     t_gen = time.perf_counter() - t_gen
+    log("generated %d x %d, nnz %d in %.1f s" % (inp.nrow, inp.ncol, inp.nnz, t_gen))
     init = datagen.start_vector(inp.ncol)
     m, n, nnz = inp.nrow, inp.ncol, inp.nnz
     opts = eng.Options(initial=init, convergence_tolerance=TOL)
@@ -215,6 +224,7 @@ def main():
     mat32 = eng.ParallelSparseMatrix(m, n, inp.val, inp.idx, inp.ptr, inp.column_major,
                                      form=eng.FORM_FP32_FP64STEPS)
     t_ing = time.perf_counter() - t_ing
+    log("ingested FP32 form in %.1f s" % t_ing)
     lay = mat32.layout()
     stream = torch.cuda.current_stream()
     dU = torch.empty(m * NUMBER, dtype=torch.float64, device="cuda")
@@ -226,9 +236,6 @@ def main():
         """One PCA step on device-resident data: statistics + compute + scores."""
         keep = []
         o = opts._to_c(keep)
-        S = np.zeros((NUMBER, m))
-        R = np.zeros((NUMBER, n))
-        var = np.zeros(NUMBER)
         num = ctypes.c_int64()
         conv = ctypes.c_int32()
         iters = ctypes.c_int32()
@@ -242,8 +249,10 @@ def main():
         eng._check(rc)
         return {"converged": bool(conv.value), "iterations": iters.value, "stats": eng._stats_dict(st)}
 
-    for _ in range(args.warmup):
-        solve(mat32)
+    for w in range(args.warmup):
+        r = solve(mat32)
+        log("warmup %d: %d restarts, converged %s, %.1f ms" % (w, r["iterations"], r["converged"],
+                                                              r["stats"]["device_ms"]))
     clocks = Clocks(local)
     barrier()
     torch.cuda.synchronize()
@@ -257,6 +266,7 @@ def main():
     prof_launch = dict(prof_ms)
     for _ in range(args.steps):
         results.append(solve(mat32, profile=True))
+        log("step: %d restarts, %.1f ms" % (results[-1]["iterations"], results[-1]["stats"]["device_ms"]))
         pr = eng.last_profile()
         for k in prof_ms:
             prof_ms[k] += pr[k]["ms"]
@@ -337,6 +347,7 @@ def main():
             mtmp.close()
             torch.cuda.synchronize()
             e2e_times.append(time.perf_counter() - t0)
+            log("e2e step %.2f s" % e2e_times[-1])
         h1, d1 = eng.transfer_bytes()
         e2e = max_over_ranks(statistics.median(e2e_times))
         out["e2e"] = {"value": e2e, "unit": "s", "h2d_bytes_per_step": (h1 - h0) // n_e2e,
@@ -348,7 +359,9 @@ def main():
         vals64 = inp.val.astype(np.float64)
         mat64 = eng.ParallelSparseMatrix(m, n, vals64, inp.idx, inp.ptr, inp.column_major, form=eng.FORM_FP64)
         del vals64
-        solve(mat64)
+        log("ingested FP64 form")
+        r = solve(mat64)
+        log("fp64 warmup: %d restarts, %.1f ms" % (r["iterations"], r["stats"]["device_ms"]))
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -369,7 +382,9 @@ def main():
     # Bounded CPU sample of the FP64 oracle on the host cores, scaled to time-to-tol.
     if not args.no_cpu and rank == 0:
         threads = os.cpu_count() or 1
+        log("cpu sample on %d threads" % threads)
         dt, steps = cpu_sample(inp, init, args.cpu_restarts, threads)
+        log("cpu sample %.1f s, %d steps" % (dt, steps))
         steps_total = out.get("fp64_gpu", {}).get("lanczos_steps", out["lanczos_steps"])
         per_step = dt / max(steps, 1)
         out["cpu_baseline"] = {"value": per_step * steps_total, "unit": "s", "cores": threads, "kind": "port",

@@ -18,7 +18,8 @@ BUILD = os.path.join(HERE, "_lib", "obj")
 CUDA_SOURCES = ["engine.cu", "spmv.cu", "vec.cu", "svd.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-O3", "-Xcompiler", "-pthread"] + ARCH
+              "-Xcompiler", "-O3", "-Xcompiler", "-pthread", "-Xcompiler", "-Wall",
+              "-Xcompiler", "-Werror=infinite-recursion"] + ARCH
 
 
 def _cuda_home():

@@ -13,6 +13,8 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -54,19 +56,19 @@ static std::atomic<int64_t> g_d2h_bytes{0};
 
 static cudaError_t h2d_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     g_h2d_bytes.fetch_add(static_cast<int64_t>(bytes));
-    return h2d_async(dst, src, bytes, s);
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
 }
 static cudaError_t d2h_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     g_d2h_bytes.fetch_add(static_cast<int64_t>(bytes));
-    return d2h_async(dst, src, bytes, s);
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
 }
 static cudaError_t h2d_sync(void* dst, const void* src, size_t bytes) {
     g_h2d_bytes.fetch_add(static_cast<int64_t>(bytes));
-    return h2d_sync(dst, src, bytes);
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
 }
 static cudaError_t d2h_sync(void* dst, const void* src, size_t bytes) {
     g_d2h_bytes.fetch_add(static_cast<int64_t>(bytes));
-    return d2h_sync(dst, src, bytes);
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
 }
 
 // ---------------------------------------------------------------------------
@@ -121,20 +123,43 @@ struct DeviceInfo {
     size_t max_smem_optin = 0;
 };
 
+// IRLBA_GB300_TRACE=1 prints the set-up and ingestion steps to stderr.
+static bool trace_on() {
+    static const bool on = [] {
+        const char* e = std::getenv("IRLBA_GB300_TRACE");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+#define TRACE(...)                                        \
+    do {                                                  \
+        if (trace_on()) {                                 \
+            std::fprintf(stderr, "[irlba_gb300] " __VA_ARGS__); \
+            std::fprintf(stderr, "\n");                   \
+            std::fflush(stderr);                          \
+        }                                                 \
+    } while (0)
+
 static DeviceInfo& device_info() {
     static thread_local DeviceInfo info;
     int dev = 0;
+    TRACE("device_info: cudaGetDevice");
     CUDA_TRY(cudaGetDevice(&dev));
     if (info.device != dev) {
         cudaDeviceProp prop;
+        TRACE("device_info: properties");
         CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
         info.device = dev;
         info.sms = prop.multiProcessorCount;
         info.max_smem_optin = prop.sharedMemPerBlockOptin;
+        TRACE("device_info: %d SMs, smem opt-in %zu; spmv attributes", info.sms, info.max_smem_optin);
         CUDA_TRY(spmv_configure(kPanelBytes));
+        TRACE("device_info: rotate attributes");
         CUDA_TRY(rotate_configure(sizeof(double) * 128 * 128));
+        TRACE("device_info: restart attributes");
         CUDA_TRY(restart_configure(info.max_smem_optin - 16384));
         CUDA_TRY(cudaGetLastError());
+        TRACE("device_info: done");
     }
     return info;
 }
@@ -159,6 +184,29 @@ static void parallel_chunks(int64_t n, F f) {
         const int64_t b = n * t / nt, e = n * (t + 1) / nt;
         pool.emplace_back([=, &f]() { f(b, e, t); });
     }
+    for (auto& th : pool) th.join();
+}
+
+// Rows [0, R) split into one contiguous range per host thread, balanced by the
+// number of nonzeros (ptr has R + 1 entries).
+template <typename F>
+static void parallel_rows(const int64_t* ptr, int64_t R, F f) {
+    const int64_t nnz = ptr[R];
+    const int nt = static_cast<int>(std::min<int64_t>(host_threads(), std::max<int64_t>(1, (nnz + R) / 65536)));
+    if (nt <= 1 || R < 2) {
+        f(0, R, 0);
+        return;
+    }
+    std::vector<int64_t> bounds(nt + 1, 0);
+    bounds[nt] = R;
+    int64_t r = 0;
+    for (int t = 1; t < nt; ++t) {
+        const int64_t target = (nnz + R) * t / nt;
+        while (r < R && ptr[r] + r < target) ++r;
+        bounds[t] = r;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back([=, &f]() { f(bounds[t], bounds[t + 1], t); });
     for (auto& th : pool) th.join();
 }
 
@@ -250,6 +298,7 @@ struct DirPlan {
 constexpr int64_t kSegCost = 8;
 
 static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirPlan& plan) {
+    TRACE("build_plan: %lld x %lld, nnz %lld", (long long)h.rows, (long long)h.cols, (long long)h.ptr[h.rows]);
     const DeviceInfo& di = device_info();
     DirPlanDev& d = plan.dev;
     d.nrows = h.rows;
@@ -291,7 +340,7 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
     if (!staged || npanels == 1) {
         for (int64_t r = 0; r <= R; ++r) segptr[r] = h.ptr[r];
         if (staged) idx16.resize(nnz); else idx32.resize(nnz);
-        parallel_chunks(R, [&](int64_t b, int64_t e, int) {
+        parallel_rows(h.ptr, R, [&](int64_t b, int64_t e, int) {
             for (int64_t s = h.ptr[b]; s < h.ptr[e]; ++s) {
                 if (staged) idx16[s] = static_cast<uint16_t>(h.idx[s]);
                 else idx32[s] = h.idx[s];
@@ -301,13 +350,13 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
     } else {
         // Count entries per (panel, row) then lay segments out panel-major.
         std::vector<int64_t> cnt(nseg, 0);
-        parallel_chunks(R, [&](int64_t b, int64_t e, int) {
+        parallel_rows(h.ptr, R, [&](int64_t b, int64_t e, int) {
             for (int64_t r = b; r < e; ++r)
                 for (int64_t s = h.ptr[r]; s < h.ptr[r + 1]; ++s) ++cnt[(h.idx[s] / pw) * R + r];
         });
         for (int64_t sg = 0; sg < nseg; ++sg) segptr[sg + 1] = segptr[sg] + cnt[sg];
         idx16.resize(nnz);
-        parallel_chunks(R, [&](int64_t b, int64_t e, int) {
+        parallel_rows(h.ptr, R, [&](int64_t b, int64_t e, int) {
             std::vector<int64_t> fill(npanels);
             for (int64_t r = b; r < e; ++r) {
                 for (int64_t p = 0; p < npanels; ++p) fill[p] = segptr[p * R + r];
@@ -324,7 +373,9 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
 
     // Balance CTAs over segments by cost = nnz + kSegCost per segment.
     d.smem_bytes = staged ? static_cast<size_t>(d.panel_width) * xbytes : 0;
+    TRACE("build_plan: occupancy query");
     const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes);
+    TRACE("build_plan: %d blocks per SM", per_sm);
     int64_t nblocks = static_cast<int64_t>(di.sms) * per_sm;
     const int64_t total_cost = nnz + kSegCost * nseg;
     nblocks = std::max<int64_t>(1, std::min<int64_t>(nblocks, std::max<int64_t>(1, total_cost / 2048)));
@@ -340,6 +391,7 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
     }
     d.nblocks = static_cast<int32_t>(nblocks);
 
+    TRACE("build_plan: upload (%lld segments, %lld nnz, %lld blocks)", (long long)nseg, (long long)nnz, (long long)nblocks);
     plan.segptr = upload(segptr.data(), segptr.size());
     if (staged) plan.idx = upload(idx16.data(), idx16.size());
     else plan.idx = upload(idx32.data(), idx32.size());
@@ -1202,9 +1254,15 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
         if (pointers[0] != 0) invalid("pointers must start at zero");
         for (int64_t p = 0; p < primary; ++p)
             if (pointers[p + 1] < pointers[p]) invalid("pointers must be non-decreasing");
-        const int64_t nnz = pointers[primary];
-        for (int64_t s = 0; s < nnz; ++s)
-            if (indices[s] < 0 || indices[s] >= secondary) invalid("index out of range of the secondary dimension");
+        std::atomic<int> bad_index{0};
+        parallel_rows(pointers, primary, [&](int64_t b, int64_t e, int) {
+            for (int64_t s = pointers[b]; s < pointers[e]; ++s)
+                if (indices[s] < 0 || indices[s] >= secondary) {
+                    bad_index.store(1);
+                    break;
+                }
+        });
+        if (bad_index.load()) invalid("index out of range of the secondary dimension");
         device_info();
         auto base = std::make_shared<BaseMatrix>();
         base->nrow = nrow;
@@ -1256,6 +1314,7 @@ irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, c
         base->store_f64 = (form == IRLBA_GB300_FORM_FP64) && in_f64;
         const bool x_f64 = form == IRLBA_GB300_FORM_FP64;
         HostCompressed byrow = dense_to_compressed(nrow, ncol, values, in_f64, ld, row_major != 0, true);
+        TRACE("create_dense: by rows done");
         HostCompressed bycol = dense_to_compressed(nrow, ncol, values, in_f64, ld, row_major != 0, false);
         build_plan(byrow, base->store_f64, x_f64, base->mul);
         build_plan(bycol, base->store_f64, x_f64, base->adj);

@@ -6,7 +6,8 @@
 // FP64, with the parallel round-robin ("circle") pair ordering so that one
 // warp rotates one disjoint column pair per round inside a single CTA.
 // Rotations use Rutishauser's formulas; a pair is skipped when
-// |g_p . g_q| <= eps * ||g_p|| ||g_q||. Singular values are the final column
+// |g_p . g_q| <= m eps ||g_p|| ||g_q|| (m = rows; the rounding floor of the
+// dot product, so sweeps terminate). Singular values are the final column
 // norms, sorted decreasingly (ties keep column order); U = G / sigma, and
 // columns of U with a zero singular value are completed to an orthonormal basis
 // by Gram-Schmidt against unit vectors.
@@ -62,7 +63,7 @@ __device__ void jacobi_sweeps(double* G, int64_t m, int n, double* V, int* sweep
                 a = warp_sum(a);
                 b = warp_sum(b);
                 g = warp_sum(g);
-                if (g == 0.0 || fabs(g) <= eps * sqrt(a * b)) continue;
+                if (g == 0.0 || fabs(g) <= eps * static_cast<double>(m) * sqrt(a * b)) continue;
                 const double zeta = (b - a) / (2.0 * g);
                 const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
                 const double c = 1.0 / sqrt(1.0 + t * t);

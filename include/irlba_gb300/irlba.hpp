@@ -1,0 +1,510 @@
+// Header-style C++ drop-in for CppIrlba's IRLBA entry points, backed by the
+// GB300 engine through the C ABI in irlba_gb300.h.
+//
+// Same names and meanings as CppIrlba (include/irlba/*.hpp):
+//   irlba::Options                      Options.hpp:19-83
+//   irlba::Matrix, Workspace,
+//     AdjointWorkspace, RealizeWorkspace Matrix/interface.hpp:23-223
+//   irlba::SimpleMatrix                 Matrix/simple.hpp:124-178 (dense input)
+//   irlba::ParallelSparseMatrix         Matrix/sparse.hpp:438-589
+//   irlba::CenteredMatrix               Matrix/centered.hpp:139-204
+//   irlba::ScaledMatrix                 Matrix/scaled.hpp:195-268
+//   irlba::compute, compute_simple,
+//     Results                           compute.hpp:141-433
+//   irlba::pca, PcaResults              pca.hpp:55-204
+// Vector and matrix types are template parameters as in the reference; they
+// need data(), size() / rows(), cols() and resize(), which Eigen's dense types
+// provide. Matrices are column-major (a type with a static `IsRowMajor` true is
+// read as row-major). Errors are std::runtime_error with the reference's
+// messages. The arithmetic form (plain FP64 or FP32 with FP64 steps) is an
+// engine setting outside Options: irlba::gpu::set_form().
+#ifndef IRLBA_GB300_IRLBA_HPP
+#define IRLBA_GB300_IRLBA_HPP
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <optional>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../irlba_gb300.h"
+
+namespace irlba {
+
+typedef std::ptrdiff_t Index;
+
+namespace gpu {
+
+inline irlba_gb300_form& default_form() {
+    static thread_local irlba_gb300_form form = IRLBA_GB300_FORM_FP64;
+    return form;
+}
+
+// Arithmetic form used by matrices constructed afterwards on this thread.
+inline void set_form(irlba_gb300_form form) { default_form() = form; }
+
+inline void check(irlba_gb300_status st) {
+    if (st != IRLBA_GB300_OK) throw std::runtime_error(irlba_gb300_last_error());
+}
+
+struct HandleDeleter {
+    void operator()(irlba_gb300_matrix* h) const {
+        if (h) irlba_gb300_matrix_destroy(h);
+    }
+};
+typedef std::shared_ptr<irlba_gb300_matrix> Handle;
+
+inline Handle adopt(irlba_gb300_matrix* h) { return Handle(h, HandleDeleter()); }
+
+template <class T, class = void>
+struct is_row_major : std::false_type {};
+template <class T>
+struct is_row_major<T, std::void_t<decltype(T::IsRowMajor)>> : std::integral_constant<bool, static_cast<bool>(T::IsRowMajor)> {};
+
+template <class P>
+auto& deref(const P& p) { return *p; }
+
+}  // namespace gpu
+
+// ---------------------------------------------------------------------------
+// Options (Options.hpp:19-83)
+// ---------------------------------------------------------------------------
+template <class EigenVector_>
+struct Options {
+    double invariant_subspace_tolerance = -1;
+    double convergence_tolerance = 1e-5;
+    double singular_value_ratio_tolerance = -1;
+    int extra_work = 7;
+    int max_iterations = 1000;
+    bool exact_for_small_matrix = true;
+    bool exact_for_large_number = true;
+    bool cap_number = false;
+    typename std::mt19937_64::result_type seed = std::mt19937_64::default_seed;
+    std::optional<EigenVector_> initial;
+};
+
+namespace gpu {
+template <class EigenVector_>
+irlba_gb300_options to_c(const Options<EigenVector_>& o, std::vector<double>& init_buf) {
+    irlba_gb300_options c;
+    irlba_gb300_default_options(&c);
+    c.invariant_subspace_tolerance = o.invariant_subspace_tolerance;
+    c.convergence_tolerance = o.convergence_tolerance;
+    c.singular_value_ratio_tolerance = o.singular_value_ratio_tolerance;
+    c.extra_work = o.extra_work;
+    c.max_iterations = o.max_iterations;
+    c.exact_for_small_matrix = o.exact_for_small_matrix;
+    c.exact_for_large_number = o.exact_for_large_number;
+    c.cap_number = o.cap_number;
+    c.seed = o.seed;
+    if (o.initial.has_value()) {
+        const auto& v = *o.initial;
+        init_buf.assign(v.data(), v.data() + v.size());
+        c.initial = init_buf.data();
+        c.initial_size = static_cast<int64_t>(init_buf.size());
+    }
+    return c;
+}
+}  // namespace gpu
+
+// ---------------------------------------------------------------------------
+// Plug-in surface (Matrix/interface.hpp)
+// ---------------------------------------------------------------------------
+template <class EigenVector_>
+class Workspace {
+public:
+    virtual ~Workspace() {}
+    virtual void multiply(const EigenVector_& right, EigenVector_& output) = 0;
+};
+
+template <class EigenVector_>
+class AdjointWorkspace {
+public:
+    virtual ~AdjointWorkspace() {}
+    virtual void multiply(const EigenVector_& right, EigenVector_& output) = 0;
+};
+
+template <class EigenMatrix_>
+class RealizeWorkspace {
+public:
+    virtual ~RealizeWorkspace() {}
+    virtual const EigenMatrix_& realize(EigenMatrix_& buffer) = 0;
+    void realize_copy(EigenMatrix_& buffer) {
+        const auto& out = realize(buffer);
+        if (&out != &buffer) buffer = out;
+    }
+};
+
+template <class EigenVector_, class EigenMatrix_>
+class Matrix {
+public:
+    virtual ~Matrix() {}
+    virtual Index rows() const = 0;
+    virtual Index cols() const = 0;
+    virtual std::unique_ptr<Workspace<EigenVector_>> new_workspace() const = 0;
+    virtual std::unique_ptr<AdjointWorkspace<EigenVector_>> new_adjoint_workspace() const = 0;
+    virtual std::unique_ptr<RealizeWorkspace<EigenMatrix_>> new_realize_workspace() const = 0;
+    std::unique_ptr<Workspace<EigenVector_>> new_known_workspace() const { return new_workspace(); }
+    std::unique_ptr<AdjointWorkspace<EigenVector_>> new_known_adjoint_workspace() const {
+        return new_adjoint_workspace();
+    }
+    std::unique_ptr<RealizeWorkspace<EigenMatrix_>> new_known_realize_workspace() const {
+        return new_realize_workspace();
+    }
+    // Device handle of the engine, or NULL for a matrix the engine cannot run.
+    virtual const irlba_gb300_matrix* gpu_handle() const { return nullptr; }
+};
+
+namespace gpu {
+
+template <class EigenVector_>
+class HandleWorkspace final : public Workspace<EigenVector_> {
+public:
+    explicit HandleWorkspace(const irlba_gb300_matrix* h) : my_h(h) {}
+    void multiply(const EigenVector_& right, EigenVector_& output) {
+        int64_t nr = 0, nc = 0;
+        check(irlba_gb300_matrix_dims(my_h, &nr, &nc));
+        std::vector<double> in(right.data(), right.data() + right.size()), out(nr);
+        check(irlba_gb300_multiply(my_h, in.data(), out.data()));
+        output.resize(nr);
+        for (int64_t i = 0; i < nr; ++i) output.data()[i] = out[i];
+    }
+
+private:
+    const irlba_gb300_matrix* my_h;
+};
+
+template <class EigenVector_>
+class HandleAdjointWorkspace final : public AdjointWorkspace<EigenVector_> {
+public:
+    explicit HandleAdjointWorkspace(const irlba_gb300_matrix* h) : my_h(h) {}
+    void multiply(const EigenVector_& right, EigenVector_& output) {
+        int64_t nr = 0, nc = 0;
+        check(irlba_gb300_matrix_dims(my_h, &nr, &nc));
+        std::vector<double> in(right.data(), right.data() + right.size()), out(nc);
+        check(irlba_gb300_adjoint_multiply(my_h, in.data(), out.data()));
+        output.resize(nc);
+        for (int64_t i = 0; i < nc; ++i) output.data()[i] = out[i];
+    }
+
+private:
+    const irlba_gb300_matrix* my_h;
+};
+
+template <class EigenMatrix_>
+class HandleRealizeWorkspace final : public RealizeWorkspace<EigenMatrix_> {
+public:
+    explicit HandleRealizeWorkspace(const irlba_gb300_matrix* h) : my_h(h) {}
+    const EigenMatrix_& realize(EigenMatrix_& buffer) {
+        int64_t nr = 0, nc = 0;
+        check(irlba_gb300_matrix_dims(my_h, &nr, &nc));
+        std::vector<double> out(static_cast<size_t>(nr * nc));
+        check(irlba_gb300_realize(my_h, out.data()));
+        buffer.resize(nr, nc);
+        for (int64_t c = 0; c < nc; ++c)
+            for (int64_t r = 0; r < nr; ++r) buffer(r, c) = out[c * nr + r];
+        return buffer;
+    }
+
+private:
+    const irlba_gb300_matrix* my_h;
+};
+
+// Common base of the engine-backed matrices.
+template <class EigenVector_, class EigenMatrix_>
+class HandleMatrix : public Matrix<EigenVector_, EigenMatrix_> {
+public:
+    Index rows() const { return my_nrow; }
+    Index cols() const { return my_ncol; }
+    std::unique_ptr<Workspace<EigenVector_>> new_workspace() const {
+        return std::make_unique<HandleWorkspace<EigenVector_>>(my_handle.get());
+    }
+    std::unique_ptr<AdjointWorkspace<EigenVector_>> new_adjoint_workspace() const {
+        return std::make_unique<HandleAdjointWorkspace<EigenVector_>>(my_handle.get());
+    }
+    std::unique_ptr<RealizeWorkspace<EigenMatrix_>> new_realize_workspace() const {
+        return std::make_unique<HandleRealizeWorkspace<EigenMatrix_>>(my_handle.get());
+    }
+    const irlba_gb300_matrix* gpu_handle() const { return my_handle.get(); }
+
+protected:
+    Handle my_handle;
+    Index my_nrow = 0, my_ncol = 0;
+};
+
+}  // namespace gpu
+
+// SimpleMatrix over a dense matrix (simple.hpp:124-178). The data are copied
+// to the device at construction.
+template <class EigenVector_, class EigenMatrix_, class Simple_>
+class SimpleMatrix final : public gpu::HandleMatrix<EigenVector_, EigenMatrix_> {
+public:
+    explicit SimpleMatrix(Simple_ matrix) : my_matrix(std::move(matrix)) {
+        const auto& m = gpu::deref(my_matrix);
+        typedef typename std::remove_cv<typename std::remove_reference<decltype(m)>::type>::type M;
+        typedef typename std::remove_cv<typename std::remove_pointer<decltype(m.data())>::type>::type Scalar;
+        const bool rm = gpu::is_row_major<M>::value;
+        irlba_gb300_matrix* h = nullptr;
+        const irlba_gb300_value_type vt = std::is_same<Scalar, float>::value ? IRLBA_GB300_VALUE_F32 : IRLBA_GB300_VALUE_F64;
+        std::vector<double> conv;
+        const void* data = m.data();
+        if (!std::is_same<Scalar, float>::value && !std::is_same<Scalar, double>::value) {
+            conv.assign(m.data(), m.data() + m.rows() * m.cols());
+            data = conv.data();
+        }
+        const int64_t ld = rm ? m.cols() : m.rows();
+        gpu::check(irlba_gb300_matrix_create_dense(m.rows(), m.cols(), data, vt, ld > 0 ? ld : 1, rm ? 1 : 0,
+                                                   gpu::default_form(), &h));
+        this->my_handle = gpu::adopt(h);
+        this->my_nrow = m.rows();
+        this->my_ncol = m.cols();
+    }
+
+private:
+    Simple_ my_matrix;
+};
+
+// ParallelSparseMatrix (sparse.hpp:469): compressed sparse column/row data.
+// num_threads is accepted for interface parity; the device sets its own split.
+template <class EigenVector_, class EigenMatrix_, class ValueArray_, class IndexArray_, class PointerArray_>
+class ParallelSparseMatrix final : public gpu::HandleMatrix<EigenVector_, EigenMatrix_> {
+public:
+    ParallelSparseMatrix() {}
+    ParallelSparseMatrix(Index nrow, Index ncol, ValueArray_ x, IndexArray_ i, PointerArray_ p, bool column_major,
+                         int num_threads)
+        : my_values(std::move(x)), my_indices(std::move(i)), my_ptrs(std::move(p)), my_column_major(column_major),
+          my_num_threads(num_threads) {
+        const Index primary = column_major ? ncol : nrow;
+        std::vector<int64_t> ptr(static_cast<size_t>(primary) + 1);
+        for (Index k = 0; k <= primary; ++k) ptr[k] = static_cast<int64_t>(my_ptrs[k]);
+        const int64_t nnz = ptr[primary];
+        std::vector<int32_t> idx(static_cast<size_t>(nnz));
+        for (int64_t k = 0; k < nnz; ++k) idx[k] = static_cast<int32_t>(my_indices[k]);
+        typedef typename std::remove_cv<typename std::remove_reference<decltype(my_values[0])>::type>::type Scalar;
+        std::vector<double> v64;
+        std::vector<float> v32;
+        const void* vals;
+        irlba_gb300_value_type vt;
+        if (std::is_same<Scalar, float>::value) {
+            v32.resize(nnz);
+            for (int64_t k = 0; k < nnz; ++k) v32[k] = static_cast<float>(my_values[k]);
+            vals = v32.data();
+            vt = IRLBA_GB300_VALUE_F32;
+        } else {
+            v64.resize(nnz);
+            for (int64_t k = 0; k < nnz; ++k) v64[k] = static_cast<double>(my_values[k]);
+            vals = v64.data();
+            vt = IRLBA_GB300_VALUE_F64;
+        }
+        irlba_gb300_matrix* h = nullptr;
+        gpu::check(irlba_gb300_matrix_create_sparse(nrow, ncol, vals, vt, idx.data(), ptr.data(), column_major ? 1 : 0,
+                                                    gpu::default_form(), &h));
+        this->my_handle = gpu::adopt(h);
+        this->my_nrow = nrow;
+        this->my_ncol = ncol;
+    }
+    const ValueArray_& get_values() const { return my_values; }
+    const IndexArray_& get_indices() const { return my_indices; }
+    const PointerArray_& get_pointers() const { return my_ptrs; }
+    bool get_column_major() const { return my_column_major; }
+    int get_num_threads() const { return my_num_threads; }
+
+private:
+    ValueArray_ my_values;
+    IndexArray_ my_indices;
+    PointerArray_ my_ptrs;
+    bool my_column_major = false;
+    int my_num_threads = 1;
+};
+
+// CenteredMatrix (centered.hpp:139-204).
+template <class EigenVector_, class EigenMatrix_, class MatrixPointer_ = const Matrix<EigenVector_, EigenMatrix_>*,
+          class CenterPointer_ = const EigenVector_*>
+class CenteredMatrix final : public gpu::HandleMatrix<EigenVector_, EigenMatrix_> {
+public:
+    CenteredMatrix(MatrixPointer_ matrix, CenterPointer_ center) : my_matrix(std::move(matrix)), my_center(std::move(center)) {
+        const auto& inner = gpu::deref(my_matrix);
+        const irlba_gb300_matrix* ih = inner.gpu_handle();
+        if (!ih) throw std::runtime_error("CenteredMatrix on the GPU engine needs an engine-backed inner matrix");
+        const auto& c = gpu::deref(my_center);
+        std::vector<double> cv(c.data(), c.data() + c.size());
+        if (static_cast<Index>(cv.size()) != inner.cols()) throw std::runtime_error("center has the wrong length");
+        irlba_gb300_matrix* h = nullptr;
+        gpu::check(irlba_gb300_matrix_center(ih, cv.data(), &h));
+        this->my_handle = gpu::adopt(h);
+        this->my_nrow = inner.rows();
+        this->my_ncol = inner.cols();
+    }
+
+private:
+    MatrixPointer_ my_matrix;
+    CenterPointer_ my_center;
+};
+
+// ScaledMatrix (scaled.hpp:195-268).
+template <class EigenVector_, class EigenMatrix_, class MatrixPointer_ = const Matrix<EigenVector_, EigenMatrix_>*,
+          class ScalePointer_ = const EigenVector_*>
+class ScaledMatrix final : public gpu::HandleMatrix<EigenVector_, EigenMatrix_> {
+public:
+    ScaledMatrix(MatrixPointer_ matrix, ScalePointer_ scale, bool column, bool divide)
+        : my_matrix(std::move(matrix)), my_scale(std::move(scale)) {
+        const auto& inner = gpu::deref(my_matrix);
+        const irlba_gb300_matrix* ih = inner.gpu_handle();
+        if (!ih) throw std::runtime_error("ScaledMatrix on the GPU engine needs an engine-backed inner matrix");
+        const auto& s = gpu::deref(my_scale);
+        std::vector<double> sv(s.data(), s.data() + s.size());
+        if (static_cast<Index>(sv.size()) != (column ? inner.cols() : inner.rows()))
+            throw std::runtime_error("scale has the wrong length");
+        irlba_gb300_matrix* h = nullptr;
+        gpu::check(irlba_gb300_matrix_scale(ih, sv.data(), column ? 1 : 0, divide ? 1 : 0, &h));
+        this->my_handle = gpu::adopt(h);
+        this->my_nrow = inner.rows();
+        this->my_ncol = inner.cols();
+    }
+
+private:
+    MatrixPointer_ my_matrix;
+    ScalePointer_ my_scale;
+};
+
+// ---------------------------------------------------------------------------
+// compute (compute.hpp:141-308) and overloads
+// ---------------------------------------------------------------------------
+namespace gpu {
+template <class EigenMatrix_>
+void fill_matrix(EigenMatrix_& out, Index nr, Index nc, const std::vector<double>& colmajor) {
+    out.resize(nr, nc);
+    for (Index c = 0; c < nc; ++c)
+        for (Index r = 0; r < nr; ++r) out(r, c) = colmajor[static_cast<size_t>(c * nr + r)];
+}
+template <class EigenVector_>
+void fill_vector(EigenVector_& out, const std::vector<double>& v, Index n) {
+    out.resize(n);
+    for (Index i = 0; i < n; ++i) out.data()[i] = v[i];
+}
+}  // namespace gpu
+
+template <class Matrix_, class EigenMatrix_, class EigenVector_>
+std::pair<bool, int> compute(const Matrix_& matrix, Index number, EigenMatrix_& outU, EigenMatrix_& outV,
+                             EigenVector_& outD, const Options<EigenVector_>& options) {
+    const irlba_gb300_matrix* h = matrix.gpu_handle();
+    if (!h) throw std::runtime_error("the GPU engine runs matrices built from its own Matrix types");
+    const Index nr = matrix.rows(), nc = matrix.cols();
+    const Index cap = std::max<Index>(std::min<Index>(number, std::min(nr, nc)), 0);
+    std::vector<double> U(static_cast<size_t>(nr * cap)), V(static_cast<size_t>(nc * cap)), D(cap > 0 ? cap : 1);
+    std::vector<double> init;
+    irlba_gb300_options o = gpu::to_c(options, init);
+    int64_t num = 0;
+    int32_t conv = 0, iters = 0;
+    gpu::check(irlba_gb300_compute(h, number, &o, U.data(), V.data(), D.data(), &num, &conv, &iters, nullptr));
+    gpu::fill_matrix(outU, nr, num, U);
+    gpu::fill_matrix(outV, nc, num, V);
+    gpu::fill_vector(outD, D, num);
+    return std::make_pair(conv != 0, static_cast<int>(iters));
+}
+
+template <class EigenMatrix_, class EigenVector_>
+struct Results {
+    EigenMatrix_ U;
+    EigenMatrix_ V;
+    EigenVector_ D;
+    int iterations;
+    bool converged;
+};
+
+template <class EigenMatrix_, class EigenVector_, class Matrix_>
+Results<EigenMatrix_, EigenVector_> compute(const Matrix_& matrix, Index number, const Options<EigenVector_>& options) {
+    Results<EigenMatrix_, EigenVector_> output;
+    const auto stats = compute(matrix, number, output.U, output.V, output.D, options);
+    output.converged = stats.first;
+    output.iterations = stats.second;
+    return output;
+}
+
+template <class InputEigenMatrix_, class OutputEigenMatrix_, class EigenVector_>
+std::pair<bool, int> compute_simple(const InputEigenMatrix_& matrix, Index number, OutputEigenMatrix_& outU,
+                                    OutputEigenMatrix_& outV, EigenVector_& outD,
+                                    const Options<EigenVector_>& options) {
+    SimpleMatrix<EigenVector_, OutputEigenMatrix_, const InputEigenMatrix_*> wrapped(&matrix);
+    return compute(wrapped, number, outU, outV, outD, options);
+}
+
+template <class OutputEigenMatrix_, class EigenVector_, class InputEigenMatrix_>
+Results<OutputEigenMatrix_, EigenVector_> compute_simple(const InputEigenMatrix_& matrix, Index number,
+                                                         const Options<EigenVector_>& options) {
+    Results<OutputEigenMatrix_, EigenVector_> output;
+    const auto stats = compute_simple(matrix, number, output.U, output.V, output.D, options);
+    output.converged = stats.first;
+    output.iterations = stats.second;
+    return output;
+}
+
+// ---------------------------------------------------------------------------
+// pca (pca.hpp:55-204)
+// ---------------------------------------------------------------------------
+template <class EigenMatrix_, class EigenVector_>
+struct PcaResults {
+    EigenMatrix_ scores;
+    EigenMatrix_ rotation;
+    EigenVector_ variances;
+    int iterations;
+    bool converged;
+};
+
+namespace gpu {
+template <class OutputEigenMatrix_, class EigenVector_>
+std::pair<bool, int> pca_on_handle(const irlba_gb300_matrix* h, Index nr, Index nc, bool center, bool scale,
+                                   Index number, OutputEigenMatrix_& scores, OutputEigenMatrix_& rotation,
+                                   EigenVector_& variances, const Options<EigenVector_>& options) {
+    const Index cap = std::max<Index>(std::min<Index>(number, std::min(nr, nc)), 0);
+    std::vector<double> S(static_cast<size_t>(nr * cap)), R(static_cast<size_t>(nc * cap)), var(cap > 0 ? cap : 1);
+    std::vector<double> init;
+    irlba_gb300_options o = to_c(options, init);
+    int64_t num = 0;
+    int32_t conv = 0, iters = 0;
+    check(irlba_gb300_pca(h, center ? 1 : 0, scale ? 1 : 0, number, &o, S.data(), R.data(), var.data(), &num, &conv,
+                          &iters, nullptr, nullptr, nullptr));
+    fill_matrix(scores, nr, num, S);
+    fill_matrix(rotation, nc, num, R);
+    fill_vector(variances, var, num);
+    return std::make_pair(conv != 0, static_cast<int>(iters));
+}
+}  // namespace gpu
+
+template <class InputEigenMatrix_, class OutputEigenMatrix_, class EigenVector_>
+std::pair<bool, int> pca(const InputEigenMatrix_& matrix, bool center, bool scale, Index number,
+                         OutputEigenMatrix_& scores, OutputEigenMatrix_& rotation, EigenVector_& variances,
+                         const Options<EigenVector_>& options) {
+    SimpleMatrix<EigenVector_, OutputEigenMatrix_, const InputEigenMatrix_*> wrapped(&matrix);
+    return gpu::pca_on_handle(wrapped.gpu_handle(), wrapped.rows(), wrapped.cols(), center, scale, number, scores,
+                              rotation, variances, options);
+}
+
+template <class OutputEigenMatrix_, class EigenVector_, class InputEigenMatrix_>
+PcaResults<OutputEigenMatrix_, EigenVector_> pca(const InputEigenMatrix_& matrix, bool center, bool scale,
+                                                 Index number, const Options<EigenVector_>& options) {
+    PcaResults<OutputEigenMatrix_, EigenVector_> output;
+    const auto stats = pca(matrix, center, scale, number, output.scores, output.rotation, output.variances, options);
+    output.converged = stats.first;
+    output.iterations = stats.second;
+    return output;
+}
+
+// Extension: pca() over an engine-backed base matrix (e.g. a ParallelSparseMatrix
+// of cells x genes), with the column statistics computed on the device.
+template <class EigenVector_, class EigenMatrix_, class OutputEigenMatrix_>
+std::pair<bool, int> pca(const gpu::HandleMatrix<EigenVector_, EigenMatrix_>& matrix, bool center, bool scale,
+                         Index number, OutputEigenMatrix_& scores, OutputEigenMatrix_& rotation,
+                         EigenVector_& variances, const Options<EigenVector_>& options) {
+    return gpu::pca_on_handle(matrix.gpu_handle(), matrix.rows(), matrix.cols(), center, scale, number, scores,
+                              rotation, variances, options);
+}
+
+}  // namespace irlba
+
+#endif

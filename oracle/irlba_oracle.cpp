@@ -399,7 +399,7 @@ void jacobi_svd_tall(Index m, Index n, const double* A, double* S, double* U, do
                 double* gq = &G[q * m];
                 const double alpha = nrm[p], beta = nrm[q];
                 const double gamma = dot(gp, gq, m);
-                if (gamma == 0 || std::abs(gamma) <= eps * std::sqrt(alpha * beta)) continue;
+                if (gamma == 0 || std::abs(gamma) <= eps * static_cast<double>(m) * std::sqrt(alpha * beta)) continue;
                 rotated = true;
                 // Rutishauser's formulas for the Jacobi rotation that zeroes gamma.
                 const double zeta = (beta - alpha) / (2 * gamma);
@@ -736,6 +736,11 @@ std::pair<bool, int> compute(const Matrix& mat, Index number, double* outU, doub
 
     // Output assembly, compute.hpp:298-305 (uses the last SVD of B, which on a
     // max-iterations exit predates the final rotation, as in the reference).
+    if (BS.empty()) {  // no restart ran (max_iterations == 0): no SVD of B exists
+        BS.assign(work, 0.0);
+        BU = Dense(work, work);
+        BV = Dense(work, work);
+    }
     for (Index j = 0; j < requested; ++j) outD[j] = BS[j];
     Dense Uo(nr, requested), Vo(nc, requested);
     rotate(W, BU, requested, Uo);

@@ -1,0 +1,128 @@
+// Exercises the header-style drop-in (include/irlba_gb300/irlba.hpp) the way a
+// CppIrlba user would: irlba::compute / compute_simple / pca over SimpleMatrix,
+// ParallelSparseMatrix and the Centered/Scaled decorators. Prints inputs and
+// outputs as JSON for tests/test_gpu_dropin.py to check against the oracle.
+#include <cmath>
+#include <cstdio>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "irlba_gb300/irlba.hpp"
+
+// Minimal column-major dense types with the Eigen members the drop-in uses.
+struct Vec {
+    std::vector<double> v;
+    Vec() {}
+    explicit Vec(std::ptrdiff_t n) : v(n) {}
+    double* data() { return v.data(); }
+    const double* data() const { return v.data(); }
+    std::ptrdiff_t size() const { return static_cast<std::ptrdiff_t>(v.size()); }
+    void resize(std::ptrdiff_t n) { v.resize(n); }
+    double& operator[](std::ptrdiff_t i) { return v[i]; }
+};
+
+struct Mat {
+    std::ptrdiff_t nr = 0, nc = 0;
+    std::vector<double> v;
+    Mat() {}
+    Mat(std::ptrdiff_t r, std::ptrdiff_t c) : nr(r), nc(c), v(r * c) {}
+    double* data() { return v.data(); }
+    const double* data() const { return v.data(); }
+    std::ptrdiff_t rows() const { return nr; }
+    std::ptrdiff_t cols() const { return nc; }
+    void resize(std::ptrdiff_t r, std::ptrdiff_t c) { nr = r; nc = c; v.assign(r * c, 0.0); }
+    double& operator()(std::ptrdiff_t r, std::ptrdiff_t c) { return v[c * nr + r]; }
+    double operator()(std::ptrdiff_t r, std::ptrdiff_t c) const { return v[c * nr + r]; }
+};
+
+static uint64_t lcg = 88172645463325252ull;
+static double next_normal() {
+    auto u = [&]() {
+        lcg = lcg * 6364136223846793005ull + 1442695040888963407ull;
+        return ((lcg >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+    };
+    const double a = u(), b = u();
+    return std::sqrt(-2.0 * std::log(a)) * std::cos(6.283185307179586 * b);
+}
+
+static void dump_vec(const char* name, const double* p, std::ptrdiff_t n, bool comma = true) {
+    std::printf("\"%s\": [", name);
+    for (std::ptrdiff_t i = 0; i < n; ++i) std::printf("%s%.17g", i ? ", " : "", p[i]);
+    std::printf("]%s\n", comma ? "," : "");
+}
+
+int main() {
+    const std::ptrdiff_t nr = 120, nc = 70;
+    Mat A(nr, nc);
+    for (auto& x : A.v) x = next_normal();
+    Vec init(nc);
+    for (auto& x : init.v) x = next_normal();
+
+    irlba::Options<Vec> opt;
+    opt.initial = init;
+    std::printf("{\n");
+    dump_vec("A_colmajor", A.data(), nr * nc);
+    dump_vec("init", init.data(), nc);
+
+    // compute over SimpleMatrix (compute.hpp:141) and compute_simple (compute.hpp:426).
+    irlba::SimpleMatrix<Vec, Mat, const Mat*> simple(&A);
+    auto res = irlba::compute<Mat, Vec>(simple, 6, opt);
+    dump_vec("compute_D", res.D.data(), res.D.size());
+    dump_vec("compute_U0", res.U.data(), nr);
+    std::printf("\"compute_iterations\": %d, \"compute_converged\": %d,\n", res.iterations, (int)res.converged);
+    auto res2 = irlba::compute_simple<Mat, Vec>(A, 6, opt);
+    dump_vec("compute_simple_D", res2.D.data(), res2.D.size());
+
+    // pca over a dense matrix (pca.hpp:197).
+    auto p = irlba::pca<Mat, Vec>(A, true, true, 5, opt);
+    dump_vec("pca_variances", p.variances.data(), p.variances.size());
+    std::printf("\"pca_iterations\": %d,\n", p.iterations);
+
+    // ParallelSparseMatrix (CSC) with a CenteredMatrix and ScaledMatrix chain.
+    std::vector<double> x;
+    std::vector<int> i;
+    std::vector<std::size_t> ptr(1, 0);
+    for (std::ptrdiff_t c = 0; c < nc; ++c) {
+        for (std::ptrdiff_t r = 0; r < nr; ++r)
+            if (((r * 7 + c * 13) % 5) == 0) {
+                x.push_back(A(r, c));
+                i.push_back(static_cast<int>(r));
+            }
+        ptr.push_back(x.size());
+    }
+    irlba::ParallelSparseMatrix<Vec, Mat, std::vector<double>, std::vector<int>, std::vector<std::size_t>> sp(
+        nr, nc, x, i, ptr, true, 4);
+    Vec center(nc), scale(nc);
+    for (std::ptrdiff_t c = 0; c < nc; ++c) {
+        center[c] = 0.01 * c;
+        scale[c] = 1.0 + 0.02 * c;
+    }
+    irlba::CenteredMatrix<Vec, Mat> cen(&sp, &center);
+    irlba::ScaledMatrix<Vec, Mat> scl(&cen, &scale, true, true);
+    auto res3 = irlba::compute<Mat, Vec>(scl, 4, opt);
+    dump_vec("chain_D", res3.D.data(), res3.D.size());
+    std::printf("\"chain_iterations\": %d,\n", res3.iterations);
+    dump_vec("sparse_x", x.data(), x.size());
+    std::vector<double> id(i.begin(), i.end()), pd(ptr.begin(), ptr.end());
+    dump_vec("sparse_i", id.data(), id.size());
+    dump_vec("sparse_p", pd.data(), pd.size());
+    dump_vec("center", center.data(), nc);
+    dump_vec("scale", scale.data(), nc);
+
+    // Workspace multiply through the plug-in surface (interface.hpp:49, :87).
+    auto w = scl.new_workspace();
+    Vec out(nr);
+    w->multiply(init, out);
+    dump_vec("chain_multiply_init", out.data(), nr);
+
+    // An error with the reference's message (compute.hpp:156).
+    std::string msg;
+    try {
+        irlba::compute<Mat, Vec>(simple, 1000, opt);
+    } catch (const std::exception& e) {
+        msg = e.what();
+    }
+    std::printf("\"error_message\": \"%s\"\n}\n", msg.c_str());
+    return 0;
+}
