@@ -21,6 +21,7 @@
 #include <random>
 #include <stdexcept>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -1528,6 +1529,88 @@ irlba_gb300_status irlba_gb300_orthogonalize_vector_device(const double* Q, int6
                                    ctrlb.as<Ctrl>(), s);
             launch_cgs_update<double>(Q, L, ldq, static_cast<int32_t>(ncols), t.as<double>(), vec, part.as<double>(),
                                       nrm.as<double>(), 0, 0, ctrlb.as<Ctrl>(), s);
+        }
+        CUDA_TRY(cudaStreamSynchronize(s));
+        CUDA_TRY(cudaGetLastError());
+    });
+}
+
+// ---------------------------------------------------------------------------
+// orthogonalize_vector without any device allocation.
+//
+// Some callers cannot call cudaMalloc/cudaFree: code that runs inside another
+// framework's memory budget (a caching allocator that has already reserved the
+// device memory), or a latency-critical loop in which cudaMalloc/cudaFree would
+// synchronize the whole device and stall other streams. For them this variant
+// keeps its scratch (the per-CTA partial dot products, the coefficients, the
+// reduction tickets and the norm) in one file-scope device array of fixed size,
+// which every GPU that loads this library holds until the process exits.
+// ---------------------------------------------------------------------------
+namespace irlba_gb300 {
+
+// 1 MiB of scratch per device.
+constexpr int64_t kNoAllocScratchDoubles = 131072;
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+// Layout of the scratch, in doubles: control block at 0 (reduction tickets and
+// abort flag, cleared on every call), the norm at 64, the coefficients t at 128,
+// then the per-CTA partials.
+constexpr int64_t kNoAllocCtrlOffset = 0;
+constexpr int64_t kNoAllocNormOffset = 64;
+constexpr int64_t kNoAllocCoefOffset = 128;
+static_assert(sizeof(Ctrl) <= 64 * sizeof(double), "control block must fit its scratch slot");
+
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_ptr[256] = {nullptr};
+
+// Device address of the scratch array for the current device, looked up once
+// per device (with that device current) and cached.
+static double* noalloc_scratch_for_current_device() {
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) invalid("device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    return g_noalloc_ptr[dev];
+}
+
+}  // namespace irlba_gb300
+
+// Same operation as irlba_gb300_orthogonalize_vector_device, with no device
+// allocation. The first call on each device looks up the scratch array's
+// device address (make that first call before any stream capture). Calls share
+// the array: calls that overlap on the GPU (other streams, other host threads)
+// race on it. Sizes beyond the scratch are rejected: it needs
+// 128 + round_up(ncols, 32) + max(ceil(L / 4096) * ncols, min(ceil(L / 256), 1216))
+// doubles out of 131072 (1 MiB), e.g. ncols = 64 allows L up to about 8 million.
+irlba_gb300_status irlba_gb300_orthogonalize_vector_device_noalloc(const double* Q, int64_t L, int64_t ldq,
+                                                                   int64_t ncols, double* vec, void* stream) {
+    return guarded([&]() {
+        if (ncols < 0 || ncols > 1024) invalid("ncols must be in [0, 1024]");
+        if (L < 0) invalid("L must be non-negative");
+        if (ldq < L) invalid("ldq is smaller than L");
+        const int64_t part_off = kNoAllocCoefOffset + round_up(std::max<int64_t>(ncols, 1), 32);
+        const int64_t part_sz = std::max<int64_t>(static_cast<int64_t>(cgs_dot_grid(L)) * std::max<int64_t>(ncols, 1),
+                                                  cgs_update_grid(L));
+        if (part_off + part_sz > kNoAllocScratchDoubles)
+            invalid("orthogonalize_vector_device_noalloc: L and ncols need " + std::to_string(part_off + part_sz) +
+                    " doubles of scratch, more than the fixed " + std::to_string(kNoAllocScratchDoubles));
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        double* scratch = noalloc_scratch_for_current_device();
+        Ctrl* ctrl = reinterpret_cast<Ctrl*>(scratch + kNoAllocCtrlOffset);
+        double* nrm = scratch + kNoAllocNormOffset;
+        double* t = scratch + kNoAllocCoefOffset;
+        double* part = scratch + part_off;
+        // The tickets and the abort flag must start at zero; the array keeps the
+        // previous call's contents.
+        CUDA_TRY(cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), s));
+        if (ncols > 0) {
+            launch_cgs_dot<double>(Q, L, ldq, static_cast<int32_t>(ncols), vec, part, t, ctrl, s);
+            launch_cgs_update<double>(Q, L, ldq, static_cast<int32_t>(ncols), t, vec, part, nrm, 0, 0, ctrl, s);
         }
         CUDA_TRY(cudaStreamSynchronize(s));
         CUDA_TRY(cudaGetLastError());

@@ -154,6 +154,18 @@ irlba_gb300_status irlba_gb300_pca(const irlba_gb300_matrix* matrix, int32_t cen
 irlba_gb300_status irlba_gb300_orthogonalize_vector_device(const double* Q, int64_t L, int64_t ldq, int64_t ncols,
                                                            double* vec, void* stream);
 
+/* Same as irlba_gb300_orthogonalize_vector_device, but allocates nothing: for
+ * callers that cannot call cudaMalloc/cudaFree (code living inside another
+ * framework's memory budget, or latency-critical loops where an allocation
+ * would synchronize the device). No counterpart in the reference. Scratch is a
+ * fixed 1 MiB device array per GPU, held until the process exits; the first
+ * call on a device looks up its address (make it before any stream capture).
+ * Calls that overlap on the GPU race on the shared scratch. Needs
+ * 128 + round_up(ncols, 32) + max(ceil(L / 4096) * ncols, min(ceil(L / 256), 1216))
+ * <= 131072 doubles; larger requests return IRLBA_GB300_ERROR_INVALID_ARGUMENT. */
+irlba_gb300_status irlba_gb300_orthogonalize_vector_device_noalloc(const double* Q, int64_t L, int64_t ldq,
+                                                                   int64_t ncols, double* vec, void* stream);
+
 /* ---- Extensions without a counterpart in the reference --------------------- */
 
 /* irlba_gb300_compute with U (nrow x number), V (ncol x number) and D (number)
