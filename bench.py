@@ -317,6 +317,7 @@ def main():
         "restarts": last["iterations"],
         "lanczos_steps": last["stats"]["lanczos_steps"],
         "matvecs": last["stats"]["matvecs"],
+        "svd_sweeps_per_restart": last["stats"]["svd_sweeps"] / max(last["iterations"], 1),
         "gpu_launches": launches,
         "kernel_ms_per_step": {k: v / args.steps for k, v in prof_ms.items()},
         "roofline": {"bound": "hbm", "kernel": "spmv (multiply + adjoint, fused centre/scale)",

@@ -62,6 +62,7 @@ class Stats(ctypes.Structure):
         ("seconds_total", ctypes.c_double),
         ("device_ms", ctypes.c_double),
         ("kernel_launches", ctypes.c_int64),
+        ("svd_sweeps", ctypes.c_int64),
     ]
 
 

@@ -158,7 +158,7 @@ static DeviceInfo& device_info() {
         TRACE("device_info: rotate attributes");
         CUDA_TRY(rotate_configure(sizeof(double) * 128 * 128));
         TRACE("device_info: restart attributes");
-        CUDA_TRY(restart_configure(info.max_smem_optin - 16384));
+        CUDA_TRY(restart_configure(info.max_smem_optin));
         CUDA_TRY(cudaGetLastError());
         TRACE("device_info: done");
     }
@@ -815,7 +815,7 @@ struct Engine {
         BS.alloc(sizeof(double) * work);
         prevS.alloc(sizeof(double) * work);
         res.alloc(sizeof(double) * work);
-        svd_scratch.alloc(sizeof(double) * 2 * work * work);
+        svd_scratch.alloc(restart_smem_bytes(work));
         CUDA_TRY(cudaMemsetAsync(V.ptr, 0, V.bytes, stream));
         CUDA_TRY(cudaMemsetAsync(W.ptr, 0, W.bytes, stream));
         CUDA_TRY(cudaMemsetAsync(B.ptr, 0, B.bytes, stream));
@@ -855,7 +855,7 @@ struct Engine {
         Result out;
         int iter = 0;
         int k = 0;
-        int64_t matvecs = 0, steps = 0, careful_restarts = 0;
+        int64_t matvecs = 0, steps = 0, careful_restarts = 0, svd_sweeps = 0;
         const DeviceInfo& di = device_info();
         const size_t restart_smem = di.max_smem_optin - 16384;
 
@@ -901,6 +901,7 @@ struct Engine {
                 if (h.null_start) throw Error(IRLBA_GB300_ERROR_NUMERICAL, "starting vector near the null space of the input matrix");
             }
             steps += work - k;
+            svd_sweeps += h.svd_sweeps;
             if (h.converged) {
                 out.converged = true;
                 break;
@@ -945,6 +946,7 @@ struct Engine {
             stats->lanczos_steps = steps;
             stats->restarts = iter + (out.converged ? 1 : 0);
             stats->careful_restarts = careful_restarts;
+            stats->svd_sweeps = svd_sweeps;
         }
         timer.collect(g_last_ms);
         for (int i = 0; i < kTNum; ++i) g_last_launches[i] = timer.launches[i];

@@ -134,7 +134,7 @@ struct RestartArgs {
     double* BV;         // work x work
     double* prevS;      // work
     double* res;        // work
-    double* scratch;    // >= 2 * work * work doubles when the SVD does not fit in shared memory
+    double* scratch;    // >= restart_smem_bytes(work) bytes, used when they exceed shared memory
     int32_t work;
     int32_t k;          // start column of the run that produced B
     int32_t requested;

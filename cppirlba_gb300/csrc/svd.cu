@@ -12,6 +12,8 @@
 // columns of U with a zero singular value are completed to an orthonormal basis
 // by Gram-Schmidt against unit vectors.
 
+#include <cooperative_groups.h>
+
 #include "kernels.cuh"
 
 namespace irlba_gb300 {
@@ -33,12 +35,21 @@ __device__ __forceinline__ int circle_partner_b(int round, int slot, int n2) {
 // One-sided Jacobi on G (m x n, column-major, ld m) accumulating V (n x n, ld n).
 // Whole CTA participates. Returns the number of sweeps in *sweeps.
 __device__ void jacobi_sweeps(double* G, int64_t m, int n, double* V, int* sweeps, int* not_converged,
-                              int* rotated_flag) {
+                              int* rotated_flag, double* nrm) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int n2 = n + (n & 1);
     const double eps = 2.220446049250313e-16;
+    const double thresh = eps * static_cast<double>(m);
     int sweep = 0;
     for (; sweep < kMaxSweeps; ++sweep) {
+        // Squared column norms, recomputed each sweep and updated per rotation
+        // (Rutishauser: ||g_p'||^2 = a - t g, ||g_q'||^2 = b + t g).
+        for (int j = warp; j < n; j += nw) {
+            double a = 0;
+            for (int64_t i = lane; i < m; i += 32) a += G[j * m + i] * G[j * m + i];
+            a = warp_sum(a);
+            if (lane == 0) nrm[j] = a;
+        }
         if (threadIdx.x == 0) *rotated_flag = 0;
         __syncthreads();
         for (int round = 0; round < n2 - 1; ++round) {
@@ -53,21 +64,24 @@ __device__ void jacobi_sweeps(double* G, int64_t m, int n, double* V, int* sweep
                 if (q >= n) continue;
                 double* gp = G + p * m;
                 double* gq = G + q * m;
-                double a = 0, b = 0, g = 0;
-                for (int64_t i = lane; i < m; i += 32) {
-                    const double x = gp[i], y = gq[i];
-                    a += x * x;
-                    b += y * y;
-                    g += x * y;
-                }
-                a = warp_sum(a);
-                b = warp_sum(b);
+                double g = 0;
+                for (int64_t i = lane; i < m; i += 32) g += gp[i] * gq[i];
                 g = warp_sum(g);
-                if (g == 0.0 || fabs(g) <= eps * static_cast<double>(m) * sqrt(a * b)) continue;
-                const double zeta = (b - a) / (2.0 * g);
-                const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                const double c = 1.0 / sqrt(1.0 + t * t);
-                const double s = c * t;
+                const double a = nrm[p], b = nrm[q];
+                if (g == 0.0 || fabs(g) <= thresh * sqrt(a * b)) continue;
+                // Rotation parameters once per pair (lane 0), then broadcast:
+                // FP64 sqrt and division are long multi-instruction sequences.
+                double c = 0, s = 0, t = 0;
+                if (lane == 0) {
+                    const double zeta = (b - a) / (2.0 * g);
+                    t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                    c = 1.0 / sqrt(1.0 + t * t);
+                    s = c * t;
+                    nrm[p] = a - t * g;
+                    nrm[q] = b + t * g;
+                }
+                c = __shfl_sync(0xffffffffu, c, 0);
+                s = __shfl_sync(0xffffffffu, s, 0);
                 for (int64_t i = lane; i < m; i += 32) {
                     const double x = gp[i], y = gq[i];
                     gp[i] = c * x - s * y;
@@ -217,26 +231,12 @@ __device__ int update_k_dev(int k, int requested, int n_converged, int work) {
     return out > 1 ? out : 1;
 }
 
-__global__ void __launch_bounds__(kSvdThreads) restart_kernel(RestartArgs a, int use_smem) {
-    extern __shared__ __align__(16) double sm[];
-    __shared__ double norms[1024];
-    __shared__ int order[1024];
-    __shared__ int rotated;
-    __shared__ int sweeps, notconv;
+// Convergence test (compute.hpp:231-264), update_k (compute.hpp:267) and the
+// rebuild of B (compute.hpp:282-293), by one CTA after the SVD of B is in
+// a.BS, a.BU, a.BV.
+__device__ void restart_tail(const RestartArgs& a, int sweeps, int notconv) {
     Ctrl* ctrl = a.ctrl;
-    if (ctrl->abort) return;
     const int n = a.work;
-    double* G = use_smem ? sm : a.scratch;
-    double* V = use_smem ? sm + n * n : a.scratch + n * n;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        G[e] = a.B[e];
-        V[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
-    }
-    __syncthreads();
-    jacobi_sweeps(G, n, n, V, &sweeps, &notconv, &rotated);
-    finish_svd(G, n, n, V, a.BS, a.BU, n, a.BV, n, norms, order);
-
-    // Convergence test, compute.hpp:231-264.
     if (threadIdx.x == 0) {
         ctrl->svd_sweeps = sweeps;
         ctrl->svd_not_converged = notconv;
@@ -270,7 +270,6 @@ __global__ void __launch_bounds__(kSvdThreads) restart_kernel(RestartArgs a, int
         }
     }
     __syncthreads();
-    // B rebuilt for the next run, compute.hpp:282-293.
     if (!ctrl->converged) {
         const int kn = ctrl->k_next;
         for (int e = threadIdx.x; e < n * n; e += blockDim.x) a.B[e] = 0.0;
@@ -280,6 +279,147 @@ __global__ void __launch_bounds__(kSvdThreads) restart_kernel(RestartArgs a, int
             a.B[l + static_cast<int64_t>(kn) * n] = a.res[l];
         }
     }
+}
+
+// Restart step on one CTA (used when the cluster form does not apply).
+__global__ void __launch_bounds__(kSvdThreads) restart_kernel(RestartArgs a, int use_smem) {
+    extern __shared__ __align__(16) double sm[];
+    __shared__ double norms[1024];
+    __shared__ int order[1024];
+    __shared__ int rotated;
+    __shared__ int sweeps, notconv;
+    Ctrl* ctrl = a.ctrl;
+    if (ctrl->abort) return;
+    const int n = a.work;
+    double* G = use_smem ? sm : a.scratch;
+    double* V = use_smem ? sm + n * n : a.scratch + n * n;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        G[e] = a.B[e];
+        V[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    jacobi_sweeps(G, n, n, V, &sweeps, &notconv, &rotated, norms);
+    finish_svd(G, n, n, V, a.BS, a.BU, n, a.BV, n, norms, order);
+    restart_tail(a, sweeps, notconv);
+}
+
+// ---------------------------------------------------------------------------
+// Restart step on a thread-block cluster. GB300 retires about two FP64 lane
+// operations per clock per SM, so one SM runs a 57 x 57 Jacobi sweep in about
+// half a millisecond. The cluster keeps G and V in CTA 0's shared memory and
+// gives each of its warps one column pair per round through distributed shared
+// memory; rounds are separated by cluster barriers. The arithmetic is the same
+// as the single-CTA form (same ordering, same formulas).
+// ---------------------------------------------------------------------------
+constexpr int kClusterCTAs = 8;
+constexpr int kClusterThreads = 128;
+constexpr int kClusterMaxRows = 128;  // per-lane register cache: 4 rows
+
+__global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kClusterThreads)
+    restart_cluster_kernel(RestartArgs a) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    extern __shared__ __align__(16) double sm[];
+    __shared__ double norms_local[kClusterMaxRows];
+    __shared__ int order[kClusterMaxRows];
+    __shared__ int rotated_local;
+    const unsigned rank = cl.block_rank();
+    const int n = a.work;
+    const int nn = n * n;
+    // The abort flag does not change while the kernel runs: every CTA takes the
+    // same branch, so no CTA waits at a barrier the others skip.
+    if (a.ctrl->abort) return;
+    double* G = cl.map_shared_rank(sm, 0);
+    double* V = G + nn;
+    double* nrm = cl.map_shared_rank(norms_local, 0);
+    int* rotated = cl.map_shared_rank(&rotated_local, 0);
+    if (rank == 0) {
+        for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+            sm[e] = a.B[e];
+            sm[nn + e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
+        }
+    }
+    cl.sync();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int gw = static_cast<int>(rank) * nw + warp;
+    const int gnw = static_cast<int>(cl.num_blocks()) * nw;
+    const int n2 = n + (n & 1);
+    const double thresh = 2.220446049250313e-16 * static_cast<double>(n);
+    int sweep = 0;
+    for (; sweep < kMaxSweeps; ++sweep) {
+        for (int j = gw; j < n; j += gnw) {
+            double s = 0;
+            for (int i = lane; i < n; i += 32) {
+                const double x = G[j * n + i];
+                s += x * x;
+            }
+            s = warp_sum(s);
+            if (lane == 0) nrm[j] = s;
+        }
+        if (rank == 0 && threadIdx.x == 0) *rotated = 0;
+        cl.sync();
+        for (int round = 0; round < n2 - 1; ++round) {
+            for (int slot = gw; slot < n2 / 2; slot += gnw) {
+                int p = circle_partner_a(round, slot, n2);
+                int q = circle_partner_b(round, slot, n2);
+                if (p > q) {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                if (q >= n) continue;
+                double* gp = G + p * n;
+                double* gq = G + q * n;
+                double xp[kClusterMaxRows / 32], xq[kClusterMaxRows / 32];
+                double g = 0;
+#pragma unroll
+                for (int u = 0; u < kClusterMaxRows / 32; ++u) {
+                    const int i = lane + 32 * u;
+                    xp[u] = i < n ? gp[i] : 0.0;
+                    xq[u] = i < n ? gq[i] : 0.0;
+                    g += xp[u] * xq[u];
+                }
+                g = warp_sum(g);
+                const double av = nrm[p], bv = nrm[q];
+                if (g == 0.0 || fabs(g) <= thresh * sqrt(av * bv)) continue;
+                double c = 0, s = 0;
+                if (lane == 0) {
+                    const double zeta = (bv - av) / (2.0 * g);
+                    const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                    c = 1.0 / sqrt(1.0 + t * t);
+                    s = c * t;
+                    nrm[p] = av - t * g;
+                    nrm[q] = bv + t * g;
+                    *rotated = 1;
+                }
+                c = __shfl_sync(0xffffffffu, c, 0);
+                s = __shfl_sync(0xffffffffu, s, 0);
+                double* vp = V + p * n;
+                double* vq = V + q * n;
+#pragma unroll
+                for (int u = 0; u < kClusterMaxRows / 32; ++u) {
+                    const int i = lane + 32 * u;
+                    if (i < n) {
+                        gp[i] = c * xp[u] - s * xq[u];
+                        gq[i] = s * xp[u] + c * xq[u];
+                        const double y = vp[i], z = vq[i];
+                        vp[i] = c * y - s * z;
+                        vq[i] = s * y + c * z;
+                    }
+                }
+            }
+            cl.sync();
+        }
+        const int any = *rotated;
+        cl.sync();
+        if (!any) break;
+    }
+    // CTA 0 finishes; the others stop touching its shared memory after the
+    // last barrier above and may exit.
+    if (rank != 0) return;
+    finish_svd(sm, n, n, sm + nn, a.BS, a.BU, n, a.BV, n, norms_local, order);
+    restart_tail(a, sweep + 1, sweep >= kMaxSweeps ? 1 : 0);
 }
 
 __global__ void __launch_bounds__(kSvdThreads) dense_svd_kernel(const double* A, int64_t m, int n, double* U, double* S,
@@ -293,7 +433,7 @@ __global__ void __launch_bounds__(kSvdThreads) dense_svd_kernel(const double* A,
     for (int64_t e = threadIdx.x; e < m * n; e += blockDim.x) G[e] = A[e];
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) VV[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
     __syncthreads();
-    jacobi_sweeps(G, m, n, VV, &sweeps, &notconv, &rotated);
+    jacobi_sweeps(G, m, n, VV, &sweeps, &notconv, &rotated, norms);
     finish_svd(G, m, n, VV, S, U, m, V, n, norms, order);
     if (threadIdx.x == 0 && ctrl) {
         ctrl->svd_sweeps = sweeps;
@@ -303,15 +443,39 @@ __global__ void __launch_bounds__(kSvdThreads) dense_svd_kernel(const double* A,
 
 }  // namespace
 
-size_t restart_smem_bytes(int work) { return sizeof(double) * 2 * static_cast<size_t>(work) * work; }
+size_t restart_smem_bytes(int work) { return 2 * sizeof(double) * static_cast<size_t>(work) * work; }
 
-cudaError_t restart_configure(size_t max_smem) {
-    return cudaFuncSetAttribute(restart_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+// Dynamic shared memory available to the restart kernel: the per-block opt-in
+// limit minus the kernel's own static shared memory.
+static size_t g_restart_max_dynamic = 0;
+
+static size_t g_restart_cluster_max_dynamic = 0;
+
+template <typename K>
+static cudaError_t allow_dynamic_smem(K kernel, size_t smem_optin, size_t* avail_out) {
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, kernel);
+    if (e != cudaSuccess) return e;
+    const size_t avail = smem_optin > attr.sharedSizeBytes ? smem_optin - attr.sharedSizeBytes : 0;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(avail));
+    if (e == cudaSuccess) *avail_out = avail;
+    return e;
 }
 
-void launch_restart(const RestartArgs& a, cudaStream_t stream, size_t max_smem) {
+cudaError_t restart_configure(size_t smem_optin) {
+    cudaError_t e = allow_dynamic_smem(restart_kernel, smem_optin, &g_restart_max_dynamic);
+    if (e == cudaSuccess) e = allow_dynamic_smem(restart_cluster_kernel, smem_optin, &g_restart_cluster_max_dynamic);
+    return e;
+}
+
+void launch_restart(const RestartArgs& a, cudaStream_t stream, size_t /*max_smem*/) {
     const size_t need = restart_smem_bytes(a.work);
-    const int use_smem = need <= max_smem ? 1 : 0;
+    if (a.work <= kClusterMaxRows && need <= g_restart_cluster_max_dynamic) {
+        restart_cluster_kernel<<<kClusterCTAs, kClusterThreads, need, stream>>>(a);
+        count_launch();
+        return;
+    }
+    const int use_smem = need <= g_restart_max_dynamic ? 1 : 0;
     restart_kernel<<<1, kSvdThreads, use_smem ? need : 0, stream>>>(a, use_smem); count_launch();
 }
 

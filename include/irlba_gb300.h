@@ -79,6 +79,7 @@ typedef struct {
     double seconds_total;     /* host wall time of the call */
     double device_ms;         /* CUDA-event time of the call on its stream */
     int64_t kernel_launches;  /* kernels this library launched during the call */
+    int64_t svd_sweeps;       /* Jacobi sweeps of the restart SVDs, summed */
 } irlba_gb300_stats;
 
 /* Opaque matrix handle: a base matrix or a centre/scale decorator over one. */
