@@ -76,7 +76,7 @@ __device__ __forceinline__ bool last_block(uint32_t* ticket, bool* flag_smem) {
     __syncthreads();
     if (threadIdx.x == 0) {
         const uint32_t t = atomicAdd(ticket, 1u);
-        *flag_smem = (t == gridDim.x - 1);
+        *flag_smem = (t == gridDim.x * gridDim.y * gridDim.z - 1);
     }
     __syncthreads();
     if (*flag_smem) __threadfence();

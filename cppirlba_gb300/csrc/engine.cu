@@ -375,7 +375,13 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
     // Balance CTAs over segments by cost = nnz + kSegCost per segment.
     d.smem_bytes = staged ? static_cast<size_t>(d.panel_width) * xbytes : 0;
     TRACE("build_plan: occupancy query");
-    const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes);
+    // Lanes per segment from the average segment length (in 16-byte vectors).
+    {
+        const double avg = nseg > 0 ? static_cast<double>(nnz) / static_cast<double>(nseg) : 0.0;
+        const double vecs = avg / (store_f64 ? 2.0 : 4.0);
+        d.group_lanes = vecs >= 96 ? 32 : vecs >= 24 ? 16 : vecs >= 6 ? 8 : 4;
+    }
+    const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes, d.group_lanes);
     TRACE("build_plan: %d blocks per SM", per_sm);
     int64_t nblocks = static_cast<int64_t>(di.sms) * per_sm;
     const int64_t total_cost = nnz + kSegCost * nseg;
@@ -1587,8 +1593,8 @@ static double* noalloc_scratch_for_current_device() {
 // device address (make that first call before any stream capture). Calls share
 // the array: calls that overlap on the GPU (other streams, other host threads)
 // race on it. Sizes beyond the scratch are rejected: it needs
-// 128 + round_up(ncols, 32) + max(ceil(L / 4096) * ncols, min(ceil(L / 256), 1216))
-// doubles out of 131072 (1 MiB), e.g. ncols = 64 allows L up to about 8 million.
+// 128 + round_up(ncols, 32) + max(ceil(L / 1024) * ncols, min(ceil(L / 256), 1216))
+// doubles out of 131072 (1 MiB), e.g. ncols = 64 allows L up to about 2 million.
 irlba_gb300_status irlba_gb300_orthogonalize_vector_device_noalloc(const double* Q, int64_t L, int64_t ldq,
                                                                    int64_t ncols, double* vec, void* stream) {
     return guarded([&]() {

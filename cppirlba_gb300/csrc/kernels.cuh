@@ -32,6 +32,7 @@ struct DirPlanDev {
     int32_t nblocks = 0;
     const int64_t* block_seg = nullptr;  // nblocks + 1 segment boundaries per CTA
     size_t smem_bytes = 0;
+    int32_t group_lanes = 32;            // lanes per segment: 4, 8, 16 or 32
 };
 
 // Fused prologue/epilogue of a matvec (deferred centring and scaling, and the
@@ -61,7 +62,7 @@ void launch_spmv(const DirPlanDev& p, const T* x, T* y, T* partial, const Epilog
 
 // Launch configuration helpers (dynamic shared-memory limits, occupancy, grids).
 cudaError_t spmv_configure(size_t max_smem);
-int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem);
+int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group);
 cudaError_t rotate_configure(size_t max_smem);
 int cgs_update_grid(int64_t L);
 int cgs_dot_grid(int64_t L);

@@ -4,10 +4,13 @@
 // Matrix/scaled.hpp:52-69,106-123 fused into the prologue and epilogue).
 //
 // Both directions are gathers over a "panel CSR" (see DirPlanDev): each CTA owns
-// a contiguous, nnz-balanced range of segments; warps take whole segments from a
-// shared counter and reduce them with lane-strided, 4-way unrolled streaming
-// loads and a warp-shuffle tree, so every output is computed in a fixed order
+// a contiguous, nnz-balanced range of segments; groups of G lanes (G = 4..32 by
+// the plan's average segment length) take whole segments from a shared counter
+// and reduce them with 16-byte vector loads of values and packed panel offsets
+// and a shuffle tree, so every output is computed in a fixed order
 // (bit-reproducible run to run). The x panel is staged in shared memory.
+
+#include <type_traits>
 
 #include "kernels.cuh"
 
@@ -30,7 +33,124 @@ __device__ __forceinline__ T apply_epilogue(T v, int64_t r, const Epilogue<T>& e
     return v;
 }
 
-template <typename VT, typename T, bool STAGED>
+// Vector widths of one 16-byte value load: 4 FP32 or 2 FP64 values, with the
+// matching packed u16 panel offsets (8 or 4 bytes) or int32 columns.
+template <typename VT>
+struct VecTraits;
+template <>
+struct VecTraits<float> {
+    static constexpr int N = 4;
+    typedef float4 V;
+    typedef uint2 I16;
+    typedef int4 I32;
+};
+template <>
+struct VecTraits<double> {
+    static constexpr int N = 2;
+    typedef double2 V;
+    typedef unsigned int I16;
+    typedef int2 I32;
+};
+
+template <typename T, bool STAGED>
+struct Gather {
+    const T* xs;              // staged panel (shared memory)
+    const T* __restrict__ x;  // global vector when not staged
+    __device__ __forceinline__ T operator()(int64_t j) const { return STAGED ? xs[j] : __ldg(x + j); }
+};
+
+// acc += sum_v val[v] * x[idx[v]] over one vector of entries, one FMA per
+// entry (a separate product sum would cost an extra add per pair on GB300's
+// narrow FP64 pipe).
+template <typename T, bool STAGED>
+__device__ __forceinline__ void vec_acc(T& acc, const float4& v, const uint2& i, const Gather<T, STAGED>& g) {
+    acc += static_cast<T>(v.x) * g(i.x & 0xffffu);
+    acc += static_cast<T>(v.y) * g(i.x >> 16);
+    acc += static_cast<T>(v.z) * g(i.y & 0xffffu);
+    acc += static_cast<T>(v.w) * g(i.y >> 16);
+}
+template <typename T, bool STAGED>
+__device__ __forceinline__ void vec_acc(T& acc, const float4& v, const int4& i, const Gather<T, STAGED>& g) {
+    acc += static_cast<T>(v.x) * g(i.x);
+    acc += static_cast<T>(v.y) * g(i.y);
+    acc += static_cast<T>(v.z) * g(i.z);
+    acc += static_cast<T>(v.w) * g(i.w);
+}
+template <typename T, bool STAGED>
+__device__ __forceinline__ void vec_acc(T& acc, const double2& v, const unsigned int& i, const Gather<T, STAGED>& g) {
+    acc += static_cast<T>(v.x) * g(i & 0xffffu);
+    acc += static_cast<T>(v.y) * g(i >> 16);
+}
+template <typename T, bool STAGED>
+__device__ __forceinline__ void vec_acc(T& acc, const double2& v, const int2& i, const Gather<T, STAGED>& g) {
+    acc += static_cast<T>(v.x) * g(i.x);
+    acc += static_cast<T>(v.y) * g(i.y);
+}
+
+// One lane's share of the segment [b, en) for a group of G lanes (glane =
+// lane within the group): a scalar head up to the first 16-byte boundary of
+// the value array, a body of vector loads (up to four per lane, all issued
+// before use), and a scalar tail. The order of the partial sums is fixed.
+template <typename VT, typename T, bool STAGED, int G>
+__device__ __forceinline__ T segment_dot(const VT* __restrict__ val, const void* idxp, const Gather<T, STAGED>& g,
+                                         int64_t b, int64_t en, int glane) {
+    typedef VecTraits<VT> VTr;
+    constexpr int N = VTr::N;
+    typedef typename VTr::V V;
+    typedef typename std::conditional<STAGED, typename VTr::I16, typename VTr::I32>::type IV;
+    typedef typename std::conditional<STAGED, uint16_t, int32_t>::type IS;
+    const IS* __restrict__ idx = static_cast<const IS*>(idxp);
+    T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    const int64_t head = min(en, (b + (N - 1)) & ~static_cast<int64_t>(N - 1));
+    if (glane < head - b) {
+        const int64_t i = b + glane;
+        a0 += static_cast<T>(ld_stream(val + i)) * g(ld_stream(idx + i));
+    }
+    const int64_t q1 = en / N;
+    int64_t q = head / N + glane;
+    const V* __restrict__ v4 = reinterpret_cast<const V*>(val);
+    const IV* __restrict__ i4 = reinterpret_cast<const IV*>(idx);
+    for (; q < q1; q += 4 * G) {
+        V va = {}, vb = {}, vc = {}, vd = {};
+        IV ia = {}, ib = {}, ic = {}, id = {};
+        const bool hb = q + G < q1, hc = q + 2 * G < q1, hd = q + 3 * G < q1;
+        va = ld_stream(v4 + q);
+        ia = ld_stream(i4 + q);
+        if (hb) {
+            vb = ld_stream(v4 + q + G);
+            ib = ld_stream(i4 + q + G);
+        }
+        if (hc) {
+            vc = ld_stream(v4 + q + 2 * G);
+            ic = ld_stream(i4 + q + 2 * G);
+        }
+        if (hd) {
+            vd = ld_stream(v4 + q + 3 * G);
+            id = ld_stream(i4 + q + 3 * G);
+        }
+        vec_acc<T, STAGED>(a0, va, ia, g);
+        if (hb) vec_acc<T, STAGED>(a1, vb, ib, g);
+        if (hc) vec_acc<T, STAGED>(a2, vc, ic, g);
+        if (hd) vec_acc<T, STAGED>(a3, vd, id, g);
+    }
+    const int64_t t0 = max(head, q1 * N);
+    if (glane < en - t0) {
+        const int64_t i = t0 + glane;
+        a2 += static_cast<T>(ld_stream(val + i)) * g(ld_stream(idx + i));
+    }
+    return (a0 + a1) + (a2 + a3);
+}
+
+template <int G, typename T>
+__device__ __forceinline__ T group_sum(T v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// G lanes per segment (32 / G segments per warp), chosen per plan from the
+// average segment length so that short rows share the per-segment bookkeeping.
+template <typename VT, typename T, bool STAGED, int G>
 __global__ void __launch_bounds__(kSpmvThreads) spmv_kernel(const DirPlanDev p, const T* __restrict__ x,
                                                             T* __restrict__ y, T* __restrict__ partial,
                                                             const Epilogue<T> e, const int32_t* abort) {
@@ -38,15 +158,21 @@ __global__ void __launch_bounds__(kSpmvThreads) spmv_kernel(const DirPlanDev p, 
     T* xs = reinterpret_cast<T*>(smem_raw);
     __shared__ unsigned int seg_counter;
     if (*abort) return;
+    constexpr int kGroups = 32 / G;
 
     EpiVals<T> ev;
     ev.beta = e.beta ? static_cast<T>(*e.beta) : T(0);
     ev.alpha = e.alpha ? static_cast<T>(*e.alpha) : T(0);
 
     const VT* __restrict__ val = static_cast<const VT*>(p.val);
+    const void* idxp = STAGED ? static_cast<const void*>(p.idx16) : static_cast<const void*>(p.idx32);
+    Gather<T, STAGED> g;
+    g.xs = xs;
+    g.x = x;
     const int64_t sb = p.block_seg[blockIdx.x];
     const int64_t se = p.block_seg[blockIdx.x + 1];
     const int lane = threadIdx.x & 31;
+    const int group = lane / G, glane = lane % G;
 
     int64_t s = sb;
     while (s < se) {
@@ -65,51 +191,38 @@ __global__ void __launch_bounds__(kSpmvThreads) spmv_kernel(const DirPlanDev p, 
         if (threadIdx.x == 0) seg_counter = 0;
         __syncthreads();
 
+        // Warps take kGroups whole segments at a time from the counter; the
+        // next batch's bounds are fetched before the current one streams.
         const unsigned int nhere = static_cast<unsigned int>(pe - s);
-        while (true) {
-            unsigned int mine = 0;
-            if (lane == 0) mine = atomicAdd(&seg_counter, 1u);
-            mine = __shfl_sync(0xffffffffu, mine, 0);
-            if (mine >= nhere) break;
-            const int64_t seg = s + mine;
-            const int64_t row = seg - panel * p.nrows;
-            const int64_t b = p.segptr[seg];
-            const int64_t en = p.segptr[seg + 1];
-            T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-            int64_t i = b + lane;
-            if (STAGED) {
-                const uint16_t* __restrict__ idx = p.idx16;
-                for (; i + 96 < en; i += 128) {
-                    const VT v0 = ld_stream(val + i), v1 = ld_stream(val + i + 32);
-                    const VT v2 = ld_stream(val + i + 64), v3 = ld_stream(val + i + 96);
-                    const uint16_t j0 = ld_stream(idx + i), j1 = ld_stream(idx + i + 32);
-                    const uint16_t j2 = ld_stream(idx + i + 64), j3 = ld_stream(idx + i + 96);
-                    a0 += static_cast<T>(v0) * xs[j0];
-                    a1 += static_cast<T>(v1) * xs[j1];
-                    a2 += static_cast<T>(v2) * xs[j2];
-                    a3 += static_cast<T>(v3) * xs[j3];
-                }
-                for (; i < en; i += 32) a0 += static_cast<T>(ld_stream(val + i)) * xs[ld_stream(idx + i)];
-            } else {
-                const int32_t* __restrict__ idx = p.idx32;
-                for (; i + 96 < en; i += 128) {
-                    const VT v0 = ld_stream(val + i), v1 = ld_stream(val + i + 32);
-                    const VT v2 = ld_stream(val + i + 64), v3 = ld_stream(val + i + 96);
-                    const int32_t j0 = ld_stream(idx + i), j1 = ld_stream(idx + i + 32);
-                    const int32_t j2 = ld_stream(idx + i + 64), j3 = ld_stream(idx + i + 96);
-                    a0 += static_cast<T>(v0) * __ldg(x + j0);
-                    a1 += static_cast<T>(v1) * __ldg(x + j1);
-                    a2 += static_cast<T>(v2) * __ldg(x + j2);
-                    a3 += static_cast<T>(v3) * __ldg(x + j3);
-                }
-                for (; i < en; i += 32) a0 += static_cast<T>(ld_stream(val + i)) * __ldg(x + ld_stream(idx + i));
+        unsigned int base = 0;
+        if (lane == 0) base = atomicAdd(&seg_counter, static_cast<unsigned int>(kGroups));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        int64_t b = 0, en = 0;
+        if (base + group < nhere) {
+            b = p.segptr[s + base + group];
+            en = p.segptr[s + base + group + 1];
+        }
+        while (base < nhere) {
+            unsigned int next = 0;
+            if (lane == 0) next = atomicAdd(&seg_counter, static_cast<unsigned int>(kGroups));
+            next = __shfl_sync(0xffffffffu, next, 0);
+            int64_t nb = 0, nen = 0;
+            if (next + group < nhere) {
+                nb = p.segptr[s + next + group];
+                nen = p.segptr[s + next + group + 1];
             }
-            T acc = (a0 + a1) + (a2 + a3);
-            acc = warp_sum(acc);
-            if (lane == 0) {
+            const unsigned int mine = base + group;
+            T acc = 0;
+            if (mine < nhere) acc = segment_dot<VT, T, STAGED, G>(val, idxp, g, b, en, glane);
+            acc = group_sum<G>(acc);
+            if (glane == 0 && mine < nhere) {
+                const int64_t row = s + mine - panel * p.nrows;
                 if (p.npanels == 1) y[row] = apply_epilogue(acc, row, e, ev);
                 else partial[panel * p.nrows + row] = acc;
             }
+            base = next;
+            b = nb;
+            en = nen;
         }
         s = pe;
     }
@@ -147,72 +260,73 @@ int grid_for(int64_t n, int threads, int cap) {
 
 }  // namespace
 
+// Calls f with the kernel instantiation for (value type, vector type, staged,
+// group lanes).
+template <typename T, typename F>
+static void with_spmv_kernel(bool vf64, bool staged, int group, F f) {
+#define IRLBA_SPMV_G(VT, ST)                                    \
+    switch (group) {                                            \
+        case 4: f(spmv_kernel<VT, T, ST, 4>); break;            \
+        case 8: f(spmv_kernel<VT, T, ST, 8>); break;            \
+        case 16: f(spmv_kernel<VT, T, ST, 16>); break;          \
+        default: f(spmv_kernel<VT, T, ST, 32>); break;          \
+    }
+    if (vf64) {
+        if (staged) { IRLBA_SPMV_G(double, true) } else { IRLBA_SPMV_G(double, false) }
+    } else {
+        if (staged) { IRLBA_SPMV_G(float, true) } else { IRLBA_SPMV_G(float, false) }
+    }
+#undef IRLBA_SPMV_G
+}
+
 template <typename T>
 void launch_spmv(const DirPlanDev& p, const T* x, T* y, T* partial, const Epilogue<T>& e, const int32_t* abort,
                  cudaStream_t stream) {
     if (p.nrows == 0) return;
-    const bool vf64 = p.val_f64 != 0;
     if (p.nblocks > 0) {
-        if (p.staged) {
-            if (vf64) {
-                spmv_kernel<double, T, true><<<p.nblocks, kSpmvThreads, p.smem_bytes, stream>>>(p, x, y, partial, e, abort); count_launch();
-            } else {
-                spmv_kernel<float, T, true><<<p.nblocks, kSpmvThreads, p.smem_bytes, stream>>>(p, x, y, partial, e, abort); count_launch();
-            }
-        } else {
-            if (vf64) {
-                spmv_kernel<double, T, false><<<p.nblocks, kSpmvThreads, 0, stream>>>(p, x, y, partial, e, abort); count_launch();
-            } else {
-                spmv_kernel<float, T, false><<<p.nblocks, kSpmvThreads, 0, stream>>>(p, x, y, partial, e, abort); count_launch();
-            }
-        }
+        const size_t smem = p.staged ? p.smem_bytes : 0;
+        with_spmv_kernel<T>(p.val_f64 != 0, p.staged != 0, p.group_lanes, [&](auto kernel) {
+            kernel<<<p.nblocks, kSpmvThreads, smem, stream>>>(p, x, y, partial, e, abort);
+        });
+        count_launch();
     }
     if (p.npanels > 1) {
         panel_reduce_kernel<T><<<grid_for(p.nrows, 256, 152 * 16), 256, 0, stream>>>(partial, p.npanels, p.nrows, y, e,
-                                                                                   abort); count_launch();
+                                                                                   abort);
+        count_launch();
     }
 }
 
 template <typename T>
 void launch_scale_vector(const T* x, const T* s, int32_t divide, int64_t n, T* out, cudaStream_t stream) {
     if (n == 0) return;
-    scale_vector_kernel<T><<<grid_for(n, 256, 152 * 16), 256, 0, stream>>>(x, s, divide, n, out); count_launch();
+    scale_vector_kernel<T><<<grid_for(n, 256, 152 * 16), 256, 0, stream>>>(x, s, divide, n, out);
+    count_launch();
 }
 
 // Raise the dynamic shared-memory limit of the staged kernels (once per device).
-template <typename K>
-static cudaError_t set_smem(K kernel, size_t bytes) {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
-}
-
 cudaError_t spmv_configure(size_t max_smem) {
-    cudaError_t e = cudaSuccess;
-    if (e == cudaSuccess) e = set_smem(spmv_kernel<float, float, true>, max_smem);
-    if (e == cudaSuccess) e = set_smem(spmv_kernel<double, double, true>, max_smem);
-    if (e == cudaSuccess) e = set_smem(spmv_kernel<float, double, true>, max_smem);
-    if (e == cudaSuccess) e = set_smem(spmv_kernel<double, float, true>, max_smem);
-    return e;
+    cudaError_t err = cudaSuccess;
+    auto set = [&](auto kernel) {
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(max_smem));
+    };
+    for (int g = 4; g <= 32; g *= 2) {
+        with_spmv_kernel<float>(false, true, g, set);
+        with_spmv_kernel<float>(true, true, g, set);
+        with_spmv_kernel<double>(false, true, g, set);
+        with_spmv_kernel<double>(true, true, g, set);
+    }
+    return err;
 }
 
-int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem) {
+int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group) {
     int nb = 0;
-    if (staged) {
-        if (tf64) {
-            if (vf64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_kernel<double, double, true>, kSpmvThreads, smem);
-            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_kernel<float, double, true>, kSpmvThreads, smem);
-        } else {
-            if (vf64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_kernel<double, float, true>, kSpmvThreads, smem);
-            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_kernel<float, float, true>, kSpmvThreads, smem);
-        }
-    } else {
-        if (tf64) {
-            if (vf64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_kernel<double, double, false>, kSpmvThreads, 0);
-            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_kernel<float, double, false>, kSpmvThreads, 0);
-        } else {
-            if (vf64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_kernel<double, float, false>, kSpmvThreads, 0);
-            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spmv_kernel<float, float, false>, kSpmvThreads, 0);
-        }
-    }
+    auto occ = [&](auto kernel) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kSpmvThreads, staged ? smem : 0);
+    };
+    if (tf64) with_spmv_kernel<double>(vf64, staged, group, occ);
+    else with_spmv_kernel<float>(vf64, staged, group, occ);
     return nb < 1 ? 1 : nb;
 }
 

@@ -11,6 +11,8 @@
 // Coefficients and norms accumulate in FP64 in both precision forms: in the FP32
 // form each lane sums 8 FP32 products before adding them to an FP64 total.
 
+#include <type_traits>
+
 #include "kernels.cuh"
 
 namespace irlba_gb300 {
@@ -18,7 +20,7 @@ namespace irlba_gb300 {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kDotRows = 4096;     // rows per CTA of the GEMV-transpose pass
+constexpr int kDotRows = 1024;     // rows per CTA of the GEMV-transpose pass
 constexpr int kMaxCols = 1024;     // basis columns held in shared memory
 
 int grid_for(int64_t n, int threads, int cap) {
@@ -31,6 +33,9 @@ int grid_for(int64_t n, int threads, int cap) {
 // ---------------------------------------------------------------------------
 // t = Q[:, :c]^T v
 // ---------------------------------------------------------------------------
+// Grid: x = chunks of kDotRows rows, y = groups of (threads / 32) columns; one
+// warp per (chunk, column). The last CTA reduces the per-chunk partials with one
+// warp per column (lane-strided over chunks, then a shuffle tree): fixed order.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) cgs_dot_kernel(const T* __restrict__ Q, int64_t L, int64_t ldq, int32_t c,
                                                            const T* __restrict__ v, double* __restrict__ part,
@@ -44,7 +49,8 @@ __global__ void __launch_bounds__(kThreads) cgs_dot_kernel(const T* __restrict__
     __syncthreads();
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int j = warp; j < c; j += nw) {
+    const int j = static_cast<int>(blockIdx.y) * nw + warp;
+    if (j < c) {
         const T* __restrict__ q = Q + j * ldq + r0;
         double acc = 0;
         int i = lane;
@@ -64,13 +70,23 @@ __global__ void __launch_bounds__(kThreads) cgs_dot_kernel(const T* __restrict__
     }
 
     if (last_block(&ctrl->ticket[kTicketDot], &is_last)) {
-        for (int j = threadIdx.x; j < c; j += blockDim.x) {
+        const int chunks = static_cast<int>(gridDim.x);
+        for (int jj = warp; jj < c; jj += nw) {
             double s = 0;
-            for (int b = 0; b < static_cast<int>(gridDim.x); ++b) s += __ldcg(part + static_cast<int64_t>(b) * c + j);
-            t[j] = s;
+            for (int b = lane; b < chunks; b += 32) s += __ldcg(part + static_cast<int64_t>(b) * c + jj);
+            s = warp_sum(s);
+            if (lane == 0) t[jj] = s;
         }
         if (threadIdx.x == 0) ctrl->ticket[kTicketDot] = 0;
     }
+}
+
+// Sum of count partials by the whole CTA in a fixed order (thread-strided, then
+// the block tree); the result is valid in thread 0.
+__device__ __forceinline__ double reduce_partials(const double* part, int count, double* red) {
+    double s = 0;
+    for (int b = threadIdx.x; b < count; b += blockDim.x) s += __ldcg(part + b);
+    return block_sum(s, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -111,9 +127,8 @@ __global__ void __launch_bounds__(kThreads) cgs_update_kernel(const T* __restric
     if (threadIdx.x == 0) part[blockIdx.x] = bs;
 
     if (last_block(&ctrl->ticket[kTicketUpdate], &is_last)) {
+        const double s = reduce_partials(part, static_cast<int>(gridDim.x), red);
         if (threadIdx.x == 0) {
-            double s = 0;
-            for (int b = 0; b < static_cast<int>(gridDim.x); ++b) s += __ldcg(part + b);
             const double nrm = sqrt(s);
             *norm_out = nrm;
             if (check_null && nrm < ctrl->eps) {
@@ -166,9 +181,8 @@ __global__ void __launch_bounds__(kThreads) normalize_kernel(T* __restrict__ v, 
     const double bs = block_sum(acc, red);
     if (threadIdx.x == 0) part[blockIdx.x] = bs;
     if (last_block(&ctrl->ticket[kTicketNormalize], &is_last)) {
+        const double s = reduce_partials(part, static_cast<int>(gridDim.x), red);
         if (threadIdx.x == 0) {
-            double s = 0;
-            for (int b = 0; b < static_cast<int>(gridDim.x); ++b) s += __ldcg(part + b);
             *beta_out = s;
             ctrl->ticket[kTicketNormalize] = 0;
         }
@@ -209,9 +223,68 @@ __global__ void __launch_bounds__(128) rotate_kernel(const T* Q, int64_t L, int6
     }
 }
 
+// FP32 rotation with the whole output row in registers: for each input column
+// j, one float4 shared-memory broadcast feeds four FMAs (the scalar form above
+// spends one shared load per FMA). R is zero-padded to WMAX x WMAX.
+template <int WMAX>
+__global__ void __launch_bounds__(128) rotate_f32_tiled_kernel(const float* Q, int64_t L, int64_t ldq, int32_t w,
+                                                               const double* __restrict__ R, int32_t ldr, int32_t k,
+                                                               float* out, int64_t ldo, const float* __restrict__ fcol,
+                                                               const double* fnorm, const int32_t* abort) {
+    __shared__ __align__(16) float4 Rs4[WMAX * (WMAX / 4)];
+    if (abort && *abort) return;
+    float* Rs = reinterpret_cast<float*>(Rs4);
+    for (int idx = threadIdx.x; idx < WMAX * WMAX; idx += blockDim.x) {
+        const int j = idx / WMAX, i = idx % WMAX;
+        Rs[idx] = (j < w && i < k) ? static_cast<float>(R[j + static_cast<int64_t>(i) * ldr]) : 0.0f;
+    }
+    __syncthreads();
+    float finv = 0;
+    if (fcol) finv = static_cast<float>(1.0 / *fnorm);
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < L;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float row[WMAX];
+#pragma unroll
+        for (int j = 0; j < WMAX; ++j) row[j] = (j < w) ? Q[r + j * ldq] : 0.0f;
+        float acc[WMAX];
+#pragma unroll
+        for (int i = 0; i < WMAX; ++i) acc[i] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < WMAX; ++j) {
+            const float rj = row[j];
+#pragma unroll
+            for (int i4 = 0; i4 < WMAX / 4; ++i4) {
+                const float4 c = Rs4[j * (WMAX / 4) + i4];
+                acc[4 * i4 + 0] += rj * c.x;
+                acc[4 * i4 + 1] += rj * c.y;
+                acc[4 * i4 + 2] += rj * c.z;
+                acc[4 * i4 + 3] += rj * c.w;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < WMAX; ++i)
+            if (i < k) out[r + i * ldo] = acc[i];
+        if (fcol) out[r + static_cast<int64_t>(k) * ldo] = fcol[r] * finv;
+    }
+}
+
 template <typename T, typename O>
 void rotate_dispatch(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, O* out,
                      int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream) {
+    if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value) {
+        if (w <= 64) {
+            const int grid = grid_for(L, 128, 152 * 16);
+            if (w <= 16) {
+                rotate_f32_tiled_kernel<16><<<grid, 128, 0, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort);
+            } else if (w <= 32) {
+                rotate_f32_tiled_kernel<32><<<grid, 128, 0, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort);
+            } else {
+                rotate_f32_tiled_kernel<64><<<grid, 128, 0, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort);
+            }
+            count_launch();
+            return;
+        }
+    }
     const int grid = grid_for(L, 128, 152 * 8);
     const int kk = k > 0 ? k : 1;
     if (w <= 16) {
@@ -318,7 +391,8 @@ template <typename T>
 void launch_cgs_dot(const T* Q, int64_t L, int64_t ldq, int32_t c, const T* v, double* part, double* t, Ctrl* ctrl,
                     cudaStream_t stream) {
     if (c <= 0 || L == 0) return;
-    const int grid = static_cast<int>((L + kDotRows - 1) / kDotRows);
+    const dim3 grid(static_cast<unsigned>((L + kDotRows - 1) / kDotRows),
+                    static_cast<unsigned>((c + kThreads / 32 - 1) / (kThreads / 32)));
     cgs_dot_kernel<T><<<grid, kThreads, 0, stream>>>(Q, L, ldq, c, v, part, t, ctrl); count_launch();
 }
 

@@ -162,7 +162,7 @@ irlba_gb300_status irlba_gb300_orthogonalize_vector_device(const double* Q, int6
  * fixed 1 MiB device array per GPU, held until the process exits; the first
  * call on a device looks up its address (make it before any stream capture).
  * Calls that overlap on the GPU race on the shared scratch. Needs
- * 128 + round_up(ncols, 32) + max(ceil(L / 4096) * ncols, min(ceil(L / 256), 1216))
+ * 128 + round_up(ncols, 32) + max(ceil(L / 1024) * ncols, min(ceil(L / 256), 1216))
  * <= 131072 doubles; larger requests return IRLBA_GB300_ERROR_INVALID_ARGUMENT. */
 irlba_gb300_status irlba_gb300_orthogonalize_vector_device_noalloc(const double* Q, int64_t L, int64_t ldq,
                                                                    int64_t ncols, double* vec, void* stream);
