@@ -34,7 +34,7 @@ TOL = 1e-5
 # with the plain FP64 GPU form, which repeats the oracle's restart count on every
 # case the tests compare). The CPU reference arm times a bounded sample of steps
 # and scales by this count.
-REFERENCE_STEPS_TO_TOL = None
+REFERENCE_STEPS_TO_TOL = 918
 
 
 T_START = time.time()

@@ -66,6 +66,37 @@ class Stats(ctypes.Structure):
     ]
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int32),
+        ("converged", ctypes.c_int32),
+        ("iterations", ctypes.c_int32),
+        ("group_mul", ctypes.c_int32),
+        ("group_adj", ctypes.c_int32),
+        ("error", ctypes.c_int32),
+        ("lanczos_steps", ctypes.c_int64),
+        ("svd_sweeps", ctypes.c_int64),
+        ("ms", ctypes.c_double),
+    ]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [
+        ("device_ms", ctypes.c_double),
+        ("tune_ms", ctypes.c_double),
+        ("single_ms", ctypes.c_double),
+        ("kernel_launches", ctypes.c_int64),
+        ("graph_captured", ctypes.c_int32),
+        ("single", ctypes.c_int32),
+        ("ctas", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
+        ("nnz", ctypes.c_int64),
+        ("lanczos_steps", ctypes.c_int64),
+    ]
+
+
+BATCH_OK, BATCH_SINGLE, BATCH_FAILED = 0, 1, 2
+
 _lib = None
 
 
@@ -114,6 +145,14 @@ def load_library():
         "irlba_gb300_last_profile": (None, [pd, ctypes.POINTER(i64)]),
         "irlba_gb300_launch_count": (i64, []),
         "irlba_gb300_transfer_bytes": (None, [ctypes.POINTER(i64), ctypes.POINTER(i64)]),
+        "irlba_gb300_batch_create": (i32, [i32, P, P, P, i32, P, P, i32, ctypes.POINTER(P)]),
+        "irlba_gb300_batch_destroy": (i32, [P]),
+        "irlba_gb300_batch_tune": (i32, [P, i32, P]),
+        "irlba_gb300_batch_groups": (i32, [P, P, P]),
+        "irlba_gb300_batch_set_groups": (i32, [P, P, P]),
+        "irlba_gb300_batch_pca": (i32, [P, i32, i32, i64, ctypes.POINTER(_Options), ctypes.POINTER(BatchStats), P]),
+        "irlba_gb300_batch_result": (i32, [P, i32, pd, pd, pd, pd, pd, ctypes.POINTER(BatchInfo)]),
+        "irlba_gb300_batch_result_device": (i32, [P, i32, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -421,3 +460,96 @@ def transfer_bytes():
     h, d = ctypes.c_int64(), ctypes.c_int64()
     load_library().irlba_gb300_transfer_bytes(ctypes.byref(h), ctypes.byref(d))
     return h.value, d.value
+
+
+class Batch:
+    """Batched form (no counterpart in the reference): many sparse matrices on
+    the device, each solved as irlba::pca(matrix_j, center, scale, number,
+    options) would solve it, in one persistent launch replayed from a captured
+    CUDA graph. `matrices` is a list of (nrow, ncol, x, i, p) compressed
+    matrices sharing `column_major` (the ParallelSparseMatrix arguments)."""
+
+    def __init__(self, matrices, column_major):
+        lib = load_library()
+        self.count = len(matrices)
+        f64 = any(np.asarray(mx[2]).dtype == np.float64 for mx in matrices)
+        dt = np.float64 if f64 else np.float32
+        self._keep = []
+        nrow = np.array([int(mx[0]) for mx in matrices], dtype=np.int64)
+        ncol = np.array([int(mx[1]) for mx in matrices], dtype=np.int64)
+        vals = (ctypes.c_void_p * max(self.count, 1))()
+        idxs = (ctypes.c_void_p * max(self.count, 1))()
+        ptrs = (ctypes.c_void_p * max(self.count, 1))()
+        for j, (_, _, x, i, pp) in enumerate(matrices):
+            x = np.ascontiguousarray(x, dtype=dt)
+            i = np.ascontiguousarray(i, dtype=np.int32)
+            pp = np.ascontiguousarray(pp, dtype=np.int64)
+            self._keep += [x, i, pp]
+            vals[j], idxs[j], ptrs[j] = x.ctypes.data, i.ctypes.data, pp.ctypes.data
+        self.nrow, self.ncol = nrow, ncol
+        h = ctypes.c_void_p()
+        _check(lib.irlba_gb300_batch_create(self.count, _vptr(nrow), _vptr(ncol), vals,
+                                            VALUE_F64 if f64 else VALUE_F32, idxs, ptrs,
+                                            int(bool(column_major)), ctypes.byref(h)))
+        self._keep = []  # the library holds its own copies
+        self._h = h
+        self._number = 0
+        self._center = self._scale = False
+
+    def close(self):
+        if self._h and self._h.value:
+            load_library().irlba_gb300_batch_destroy(self._h)
+            self._h = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def groups(self):
+        gm = np.zeros(max(self.count, 1), dtype=np.int32)
+        ga = np.zeros(max(self.count, 1), dtype=np.int32)
+        _check(load_library().irlba_gb300_batch_groups(self._h, _vptr(gm), _vptr(ga)))
+        return gm[:self.count], ga[:self.count]
+
+    def set_groups(self, group_mul=None, group_adj=None):
+        gm = None if group_mul is None else np.ascontiguousarray(group_mul, dtype=np.int32)
+        ga = None if group_adj is None else np.ascontiguousarray(group_adj, dtype=np.int32)
+        _check(load_library().irlba_gb300_batch_set_groups(self._h, None if gm is None else _vptr(gm),
+                                                           None if ga is None else _vptr(ga)))
+
+    def tune(self, repeats=3, stream=None):
+        _check(load_library().irlba_gb300_batch_tune(self._h, repeats, stream))
+
+    def pca(self, center, scale, number, options=None, stream=None):
+        """Solve every matrix; returns the call's statistics (a dict)."""
+        options = options or Options()
+        keep = []
+        o = options._to_c(keep)
+        st = BatchStats()
+        _check(load_library().irlba_gb300_batch_pca(self._h, int(bool(center)), int(bool(scale)), number,
+                                                    ctypes.byref(o), ctypes.byref(st), stream))
+        self._number, self._center, self._scale = number, bool(center), bool(scale)
+        return {f: getattr(st, f) for f, _ in BatchStats._fields_ if f != "reserved0"}
+
+    def result(self, j):
+        """PcaResults of matrix j from the last pca() call (info in .stats)."""
+        if not 0 <= j < self.count:
+            # The library reports the error (index or missing results).
+            _check(load_library().irlba_gb300_batch_result(self._h, j, None, None, None, None, None, None))
+        m, n = int(self.nrow[j]), int(self.ncol[j])
+        r = max(min(self._number, min(m, n)), 0)
+        S = np.zeros((max(self._number, 1), m))
+        R = np.zeros((max(self._number, 1), n))
+        var = np.zeros(max(self._number, 1))
+        c_out = np.zeros(max(n, 1))
+        s_out = np.zeros(max(n, 1))
+        inf = BatchInfo()
+        _check(load_library().irlba_gb300_batch_result(self._h, j, _dptr(S), _dptr(R), _dptr(var), _dptr(c_out),
+                                                       _dptr(s_out), ctypes.byref(inf)))
+        info = {f: getattr(inf, f) for f, _ in BatchInfo._fields_}
+        return PcaResults(scores=S[:r].T.copy(), rotation=R[:r].T.copy(), variances=var[:r].copy(),
+                          iterations=inf.iterations, converged=bool(inf.converged),
+                          center=c_out[:n].copy() if self._center else None,
+                          scale=s_out[:n].copy() if self._scale else None, stats=info)

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 BUILD = os.path.join(HERE, "_lib", "obj")
 
-CUDA_SOURCES = ["engine.cu", "spmv.cu", "vec.cu", "svd.cu"]
+CUDA_SOURCES = ["engine.cu", "spmv.cu", "vec.cu", "svd.cu", "batch.cu", "batch_host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O3", "-Xcompiler", "-pthread", "-Xcompiler", "-Wall",
@@ -50,7 +50,7 @@ def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
-    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h", ".hpp"))]
     headers.append(os.path.join(HERE, "..", "include", "irlba_gb300.h"))
 
     lib = os.path.join(OUT, "libirlba_gb300.so")

@@ -153,4 +153,79 @@ cudaError_t restart_configure(size_t max_smem);
 void launch_dense_svd(const double* A, int64_t m, int64_t n, double* U, double* S, double* V, double* scratch,
                       Ctrl* ctrl, cudaStream_t stream);
 
+// ---------------------------------------------------------------------------
+// Batched form (batch.cu): one persistent launch solves many independent
+// centred/scaled sparse PCAs in the FP32 form, one CTA per problem.
+// ---------------------------------------------------------------------------
+// One gather direction of one problem: plain CSR over `rows` output entries.
+// Row 0 of ptr starts at a multiple of 4 entries (16-byte aligned values).
+struct BatchDir {
+    int64_t rows = 0;
+    int64_t cols = 0;                  // length of the gathered vector
+    const int64_t* ptr = nullptr;      // rows + 1 absolute offsets into idx / val
+    const void* idx = nullptr;         // u16 columns when staged, int32 otherwise
+    const float* val = nullptr;
+    int32_t staged = 0;                // gathered vector copied to shared memory
+    int32_t group = 32;                // lanes per row: 4, 8, 16 or 32
+};
+
+struct BatchProblem {
+    int64_t m = 0, n = 0;              // rows (observations), columns (features)
+    BatchDir mul;                      // rows = m, gathers x (n)
+    BatchDir adj;                      // rows = n, gathers y (m)
+    float* V = nullptr;                // n x work, ld ldv
+    int64_t ldv = 0;
+    float* W = nullptr;                // m x work, ld ldw
+    int64_t ldw = 0;
+    float* F = nullptr;                // n
+    float* Wn = nullptr;               // m
+    float* xs = nullptr;               // n: scaled x when the multiply is not staged
+    float* center = nullptr;           // n, FP32 copies used by the matvecs
+    float* scale = nullptr;            // n
+    double* center64 = nullptr;        // n, FP64 column statistics (outputs)
+    double* scale64 = nullptr;         // n
+    const double* init = nullptr;      // n, start vector
+    double* scores = nullptr;          // m x number (ld m)
+    double* rotation = nullptr;        // n x number (ld n)
+    double* variances = nullptr;       // number
+};
+
+struct BatchParams {
+    int32_t number = 0;
+    int32_t work = 0;
+    int32_t max_iter = 0;
+    int32_t center = 0;
+    int32_t scale = 0;
+    double tol = 0;
+    double svtol = 0;
+    double eps = 0;
+};
+
+// status: 0 = finished (converged or out of iterations), 2 = a Lanczos norm
+// fell below the invariant-subspace tolerance (re-solved by the caller).
+struct BatchResult {
+    int32_t status = 0;
+    int32_t converged = 0;
+    int32_t iterations = 0;
+    int32_t svd_sweeps = 0;
+    int64_t steps = 0;
+    uint64_t t_start = 0;              // %globaltimer (ns) when the CTA took the problem
+    uint64_t t_end = 0;
+};
+
+constexpr int kBatchMaxWork = 32;
+// Largest gathered vector that a batched SpMV stages in shared memory (floats).
+int64_t batch_stage_limit();
+// Dynamic shared memory of the batched kernels for a given largest staged vector.
+size_t batch_smem_bytes(int64_t max_staged);
+cudaError_t batch_configure(size_t max_smem_optin);
+void launch_batch_pca(const BatchProblem* probs, const int32_t* order, int32_t count, const BatchParams& prm,
+                      BatchResult* results, uint32_t* queue, int grid, size_t smem, cudaStream_t stream);
+// Autotuner probe: CTAs take the problems in `order` and time `reps` SpMVs of
+// each (direction adjoint, `group` lanes per row), writing the best time in SM
+// cycles to cycles_out[problem]. Uses the problems' xs/Wn/F as scratch.
+void launch_batch_spmv_probe(const BatchProblem* probs, const int32_t* order, int32_t count, int32_t adjoint,
+                             int32_t group, int32_t reps, uint64_t* cycles_out, int grid, size_t smem,
+                             cudaStream_t stream);
+
 }  // namespace irlba_gb300

@@ -139,6 +139,13 @@ def batched_sizes(count=256, seed=4, lo=200, hi=50000, median=5000.0, sigma=1.0)
     return np.clip(n, lo, hi).astype(np.int64)
 
 
+def scrna_batch(sizes, genes=2000, density=0.08, seed=4, dtype=np.float32, cell_major=False):
+    """One cells x genes PCA input per entry of `sizes` (cells), same value model
+    as scrna_pca_input; matrix j uses seed + 1000 + j."""
+    return [scrna_pca_input(genes, int(c), density, seed + 1000 + j, dtype, cell_major)
+            for j, c in enumerate(sizes)]
+
+
 def adjoint_dense(nr=4096, nc=1024, seed=5, noise_sd=0.01):
     rng = np.random.default_rng(seed)
     k = min(nr, nc)

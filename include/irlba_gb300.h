@@ -210,6 +210,88 @@ int64_t irlba_gb300_launch_count(void);
  * process started (either pointer may be NULL). */
 void irlba_gb300_transfer_bytes(int64_t* h2d, int64_t* d2h);
 
+/* ------------------------------------------------------------------------
+ * Batched form. No counterpart in the reference, which solves one matrix per
+ * irlba::pca call (pca.hpp:55-139): a batch holds many independent sparse
+ * matrices on the device and solves them all with the same arguments, as a
+ * loop of irlba::pca(matrix_j, center, scale, number, options) would, in one
+ * persistent kernel launch replayed from a captured CUDA graph (one CTA per
+ * matrix, largest first; FP32 matrices and bases with FP64 recurrence, small
+ * SVD and convergence test). The gather schedule of each matrix's SpMVs (lanes
+ * per row) is picked by an autotuner that times the candidates on the device.
+ * Matrices whose iterations hit an invariant subspace, or whose arguments need
+ * the exact SVD or a working subspace above 32, are solved by the
+ * single-matrix FP32 form instead (status IRLBA_GB300_BATCH_SINGLE).
+ * ---------------------------------------------------------------------- */
+typedef struct irlba_gb300_batch irlba_gb300_batch;
+
+enum {
+    IRLBA_GB300_BATCH_OK = 0,      /* solved by the batched kernel */
+    IRLBA_GB300_BATCH_SINGLE = 1,  /* solved by the single-matrix engine */
+    IRLBA_GB300_BATCH_FAILED = 2   /* the single-matrix engine raised an error */
+};
+
+typedef struct {
+    int32_t status;          /* IRLBA_GB300_BATCH_* */
+    int32_t converged;
+    int32_t iterations;      /* restart iterations, as Results::iterations */
+    int32_t group_mul;       /* lanes per row of the multiply SpMV */
+    int32_t group_adj;       /* lanes per row of the adjoint SpMV */
+    int32_t error;           /* irlba_gb300_status of a failed single-matrix solve */
+    int64_t lanczos_steps;
+    int64_t svd_sweeps;
+    double ms;               /* device time of this matrix on its CTA */
+} irlba_gb300_batch_info;
+
+typedef struct {
+    double device_ms;        /* CUDA-event time of the graph launch */
+    double tune_ms;          /* autotuner time in this call (0 when cached) */
+    double single_ms;        /* time spent in single-matrix solves */
+    int64_t kernel_launches; /* kernels this library launched during the call */
+    int32_t graph_captured;  /* 1 if this call captured a new graph */
+    int32_t single;          /* matrices solved by the single-matrix engine */
+    int32_t ctas;            /* CTAs of the persistent launch */
+    int32_t reserved0;
+    int64_t nnz;             /* stored entries over all matrices (one direction) */
+    int64_t lanczos_steps;   /* summed over the batched matrices */
+} irlba_gb300_batch_stats;
+
+/* count matrices; matrix j is nrow[j] x ncol[j] in compressed form (as
+ * irlba_gb300_matrix_create_sparse), values FP32 or FP64 (stored as FP32). */
+irlba_gb300_status irlba_gb300_batch_create(int32_t count, const int64_t* nrow, const int64_t* ncol,
+                                            const void* const* values, irlba_gb300_value_type value_type,
+                                            const int32_t* const* indices, const int64_t* const* pointers,
+                                            int32_t column_major, irlba_gb300_batch** out);
+irlba_gb300_status irlba_gb300_batch_destroy(irlba_gb300_batch* batch);
+
+/* Runs the autotuner now (otherwise the first solve does): `repeats` timed
+ * SpMVs per candidate and direction. */
+irlba_gb300_status irlba_gb300_batch_tune(irlba_gb300_batch* batch, int32_t repeats, void* stream);
+/* Lanes per row chosen for each matrix (arrays of `count`, either may be NULL). */
+irlba_gb300_status irlba_gb300_batch_groups(const irlba_gb300_batch* batch, int32_t* group_mul,
+                                            int32_t* group_adj);
+/* Fixes the lanes per row (4, 8, 16 or 32) instead of tuning; NULL keeps a direction's choice. */
+irlba_gb300_status irlba_gb300_batch_set_groups(irlba_gb300_batch* batch, const int32_t* group_mul,
+                                                const int32_t* group_adj);
+
+/* pca() of every matrix, results kept on the device (fetch them with
+ * irlba_gb300_batch_result / _result_device). Issued on `stream` (NULL = an
+ * internal stream); returns when all results are complete. */
+irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* batch, int32_t center, int32_t scale, int64_t number,
+                                         const irlba_gb300_options* options, irlba_gb300_batch_stats* stats,
+                                         void* stream);
+
+/* Results of matrix `index` of the last batch_pca, copied to host memory:
+ * scores (nrow x number), rotation (ncol x number), variances (number),
+ * center and scale (ncol, when requested); any pointer may be NULL. */
+irlba_gb300_status irlba_gb300_batch_result(const irlba_gb300_batch* batch, int32_t index, double* scores,
+                                            double* rotation, double* variances, double* center, double* scale,
+                                            irlba_gb300_batch_info* info);
+/* Device addresses of the same results (valid until the next batch_pca or destroy). */
+irlba_gb300_status irlba_gb300_batch_result_device(const irlba_gb300_batch* batch, int32_t index,
+                                                   const double** scores, const double** rotation,
+                                                   const double** variances);
+
 #ifdef __cplusplus
 }
 #endif
