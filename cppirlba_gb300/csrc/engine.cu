@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "host.hpp"
+#include "matrix.hpp"
 
 namespace irlba_gb300 {
 
@@ -148,10 +149,6 @@ static void transpose_host(const HostCompressed& in, HostCompressed& out) {
 }
 
 // A device gather plan with the buffers it owns.
-struct DirPlan {
-    DirPlanDev dev;
-    DevBuf segptr, idx, val, block_seg;
-};
 
 // Relative cost of a segment against one nonzero when balancing CTAs.
 constexpr int64_t kSegCost = 8;
@@ -273,65 +270,6 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
 // ---------------------------------------------------------------------------
 // Matrix handles
 // ---------------------------------------------------------------------------
-struct BaseMatrix {
-    int64_t nrow = 0, ncol = 0;
-    irlba_gb300_form form = IRLBA_GB300_FORM_FP64;
-    bool store_f64 = true;
-    DirPlan mul;  // rows = nrow, x = ncol
-    DirPlan adj;  // rows = ncol, x = nrow
-};
-
-}  // namespace irlba_gb300
-
-struct irlba_gb300_matrix {
-    int kind = 0;  // 0 base, 1 centre, 2 scale
-    const irlba_gb300_matrix* inner = nullptr;
-    std::shared_ptr<irlba_gb300::BaseMatrix> base;
-    std::vector<double> vec;
-    int column = 1, divide = 1;
-    int64_t nrow = 0, ncol = 0;
-    irlba_gb300_form form = IRLBA_GB300_FORM_FP64;
-};
-
-namespace irlba_gb300 {
-
-// Decorator chain flattened for the fused kernels.
-struct Chain {
-    const BaseMatrix* base = nullptr;
-    const std::vector<double>* center = nullptr;
-    const std::vector<double>* scale = nullptr;
-    int scale_column = 1, scale_divide = 1;
-    int center_outer = 0;
-};
-
-static Chain flatten(const irlba_gb300_matrix* m) {
-    std::vector<const irlba_gb300_matrix*> decos;
-    const irlba_gb300_matrix* cur = m;
-    while (cur && cur->kind != 0) {
-        decos.push_back(cur);
-        cur = cur->inner;
-    }
-    if (!cur) invalid("matrix handle has no base matrix");
-    Chain ch;
-    ch.base = cur->base.get();
-    int ncenter = 0, nscale = 0;
-    for (auto* d : decos) (d->kind == 1 ? ncenter : nscale)++;
-    if (ncenter > 1 || nscale > 1)
-        throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
-                    "the GPU engine fuses at most one CenteredMatrix and one ScaledMatrix over a base matrix");
-    for (auto* d : decos) {
-        if (d->kind == 1) ch.center = &d->vec;
-        else {
-            ch.scale = &d->vec;
-            ch.scale_column = d->column;
-            ch.scale_divide = d->divide;
-        }
-    }
-    // decos[0] is outermost.
-    if (ncenter == 1 && nscale == 1) ch.center_outer = (decos[0]->kind == 1) ? 1 : 0;
-    return ch;
-}
-
 // ---------------------------------------------------------------------------
 // Optional per-kernel-class timing with CUDA events on the engine stream.
 // ---------------------------------------------------------------------------

@@ -213,6 +213,40 @@ struct BatchResult {
     uint64_t t_end = 0;
 };
 
+// ---------------------------------------------------------------------------
+// Differentiation form (adjoint.cu). Blocks are row-major FP64 with k <= 64
+// columns; Z1 and Z2 have kk = 2k <= 128.
+// ---------------------------------------------------------------------------
+constexpr int kAdjointMaxK = 64;
+// Y (plan rows x k) = plan * X (plan cols x k), k <= 128.
+void launch_spmm(const DirPlanDev& p, const double* X, int k, double* Y, cudaStream_t s);
+// Partial-buffer length (in units of k*k doubles) the reductions below need.
+int gram_parts(int64_t L);
+// out (k x k, [a * k + b]) = P^T Q over L rows; part >= gram_parts(L) * k * k doubles.
+void launch_gram(const double* P, const double* Q, int64_t L, int k, double* part, double* out, cudaStream_t s);
+// out[c] = sum_r w(r) P[r, c] (Q ? Q[r, c] : 1), k <= 128; part >= gram_parts(L) * k doubles.
+void launch_coldot(const double* P, const double* Q, const double* weight, int64_t L, int k, double* part, double* out,
+                   cudaStream_t s);
+// out = alpha * A R + beta * diag(bs) B (per column); out may alias B.
+void launch_block_update(int64_t L, int ka, int kout, const double* A, int64_t lda, const double* R, double alpha,
+                         const double* B, int64_t ldb, const double* bs, double beta, double* out, int64_t ldo,
+                         cudaStream_t s);
+void launch_rank1(int64_t L, int k, const double* a, const double* b, double coef, double* Y, cudaStream_t s);
+void launch_scale_rows(int64_t L, int k, const double* X, const double* sv, int divide, double* out, cudaStream_t s);
+void launch_cg_step(int64_t L, int k, const double* alpha, const double* P, const double* Q, double* X, double* R,
+                    cudaStream_t s);
+void launch_cg_dir(int64_t L, int k, const double* beta, const double* R, double* P, cudaStream_t s);
+void launch_shift(int64_t L, int k, const double* shift, const double* P, const double* W, double* Q, cudaStream_t s);
+void launch_to_rows(int64_t L, int k, const double* src, int64_t ld, double* out, cudaStream_t s);
+// d[r] = coef * X[r, :] . (Y ? Y[r, :] : y)
+void launch_rowdot(int64_t L, int k, const double* X, const double* Y, const double* y, double coef, double* d,
+                   cudaStream_t s);
+void launch_outer(int64_t m, int64_t n, int kk, const double* Z1, const double* Z2, void* G, int64_t ldg,
+                  int row_major, int f64, cudaStream_t s);
+void launch_sddmm(int64_t nprimary, const int64_t* ptr, const int32_t* idx, const void* vals, int f64,
+                  int column_major, const double* Z1, const double* Z2, int kk, const double* f, const double* cmean,
+                  const double* c, const double* qf, void* grad, cudaStream_t s);
+
 constexpr int kBatchMaxWork = 32;
 // Largest gathered vector that a batched SpMV stages in shared memory (floats).
 int64_t batch_stage_limit();

@@ -146,13 +146,14 @@ def scrna_batch(sizes, genes=2000, density=0.08, seed=4, dtype=np.float32, cell_
             for j, c in enumerate(sizes)]
 
 
-def adjoint_dense(nr=4096, nc=1024, seed=5, noise_sd=0.01):
+def adjoint_dense(nr=4096, nc=1024, seed=5, noise_sd=0.01, dtype=np.float32):
+    """Planted spectrum sigma_i = 50 / i plus iid N(0, noise_sd^2) noise."""
     rng = np.random.default_rng(seed)
     k = min(nr, nc)
     U0, _ = np.linalg.qr(rng.standard_normal((nr, k)))
     V0, _ = np.linalg.qr(rng.standard_normal((nc, k)))
     sv = 50.0 / np.arange(1, k + 1)
-    return ((U0 * sv) @ V0.T + noise_sd * rng.standard_normal((nr, nc))).astype(np.float32)
+    return ((U0 * sv) @ V0.T + noise_sd * rng.standard_normal((nr, nc))).astype(dtype)
 
 
 def start_vector(n, seed=12345):

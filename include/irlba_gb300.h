@@ -211,6 +211,48 @@ int64_t irlba_gb300_launch_count(void);
 void irlba_gb300_transfer_bytes(int64_t* h2d, int64_t* d2h);
 
 /* ------------------------------------------------------------------------
+ * Differentiation form. No counterpart in the reference (irlba::compute has
+ * no derivative). For the top-k SVD A' ~ U diag(S) V^T computed on `matrix`
+ * (an undecorated matrix or its centre/scale chain) and the cotangents gU
+ * (m x k), gS (k), gV (n x k) of a scalar loss, the gradient with respect to
+ * A' is the rank-2k product Z1 Z2^T. U, V, gU, gV are column-major (ld m / n)
+ * FP64 device arrays, S and gS FP64 device vectors; gU, gS or gV may be NULL
+ * (zero). The in-subspace terms are Townsend's F-matrix terms; the terms in
+ * the orthogonal complement of U and V are solved exactly by shifted
+ * conjugate gradients on the device to relative residual cg_tol (which needs
+ * S[k-1] above the (k+1)-th singular value); cg_tol < 0 uses the rank-k
+ * projection terms (I - UU^T) gU S^-1 V^T + U S^-1 gV^T (I - VV^T) instead,
+ * exact only when A' has rank k. k <= 64.
+ * ---------------------------------------------------------------------- */
+
+/* Z1 (m x 2k) and Z2 (n x 2k), row-major FP64 device arrays. */
+irlba_gb300_status irlba_gb300_svd_adjoint_factors(const irlba_gb300_matrix* matrix, int64_t k, const double* U,
+                                                   const double* S, const double* V, const double* gU,
+                                                   const double* gS, const double* gV, double cg_tol,
+                                                   int32_t cg_max_iter, double* Z1, double* Z2,
+                                                   int32_t* cg_iterations, void* stream);
+
+/* grad = Z1 Z2^T as a dense m x n device array of `type` (row-major when
+ * row_major, else column-major; leading dimension ld). */
+irlba_gb300_status irlba_gb300_svd_adjoint_dense(int64_t m, int64_t n, int64_t k, const double* Z1, const double* Z2,
+                                                 void* grad, int64_t ld, int32_t row_major,
+                                                 irlba_gb300_value_type type, void* stream);
+
+/* Gradient with respect to the stored values of a sparse input (the same
+ * compressed layout as irlba_gb300_matrix_create_sparse, as device arrays):
+ * Z1 Z2^T sampled on the sparsity pattern (SDDMM) and carried back through the
+ * chain of `matrix`: column scaling divides (or multiplies) by the scale, a
+ * constant centre adds nothing. statistics = 1 treats the centre and scale as
+ * pca()'s column means and standard deviations of these values
+ * (pca.hpp:85-109) and adds their derivatives. grad_values has the input's
+ * value type. */
+irlba_gb300_status irlba_gb300_svd_adjoint_sparse(const irlba_gb300_matrix* matrix, int64_t k, const double* Z1,
+                                                  const double* Z2, const int64_t* pointers, const int32_t* indices,
+                                                  const void* values, irlba_gb300_value_type type,
+                                                  int32_t column_major, int32_t statistics, void* grad_values,
+                                                  void* stream);
+
+/* ------------------------------------------------------------------------
  * Batched form. No counterpart in the reference, which solves one matrix per
  * irlba::pca call (pca.hpp:55-139): a batch holds many independent sparse
  * matrices on the device and solves them all with the same arguments, as a
