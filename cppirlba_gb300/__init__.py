@@ -73,7 +73,10 @@ class BatchInfo(ctypes.Structure):
         ("iterations", ctypes.c_int32),
         ("group_mul", ctypes.c_int32),
         ("group_adj", ctypes.c_int32),
+        ("prefetch_mul", ctypes.c_int32),
+        ("prefetch_adj", ctypes.c_int32),
         ("error", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
         ("lanczos_steps", ctypes.c_int64),
         ("svd_sweeps", ctypes.c_int64),
         ("ms", ctypes.c_double),

@@ -39,6 +39,7 @@ struct Persist {
     double res[kWM];
     double t[kWM];
     double norms[kWM];
+    double pairs[3 * (kWM / 2)];
     double red[kBW * kWM];
     float t32[kWM];
     float R32[kWM * kWM];
@@ -69,6 +70,26 @@ __device__ double cta_sum(double v, Persist& ps) {
     return r;
 }
 
+// Bulk prefetch of bytes [a, a + n) into L2 (no registers, no shared memory);
+// the range is widened to 16-byte boundaries, which stay inside the pooled
+// allocations (16-byte aligned, padded).
+__device__ __forceinline__ void prefetch_l2(const void* a, size_t n) {
+    uintptr_t b = reinterpret_cast<uintptr_t>(a) & ~static_cast<uintptr_t>(15);
+    const uintptr_t e = (reinterpret_cast<uintptr_t>(a) + n + 15) & ~static_cast<uintptr_t>(15);
+    for (; b < e; b += 32768) {
+        const uint32_t sz = static_cast<uint32_t>(e - b < 32768 ? e - b : 32768);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b), "r"(sz) : "memory");
+    }
+}
+
+// Values and indices of rows [ra, rb) of d into L2.
+__device__ __forceinline__ void prefetch_rows(const BatchDir& d, int64_t ra, int64_t rb) {
+    const int64_t b = d.ptr[ra], e = d.ptr[rb];
+    if (e <= b) return;
+    prefetch_l2(d.val + b, sizeof(float) * static_cast<size_t>(e - b));
+    prefetch_l2(static_cast<const char*>(d.idx) + b * d.idx_bytes, static_cast<size_t>(d.idx_bytes) * (e - b));
+}
+
 // y[r] = epi(sum_s val[s] x[idx[s]]) over the rows of d, G lanes per row:
 //   epi(v) = ((v - beta * (cvec ? cvec[r] : 1)) / (oscale ? oscale[r] : 1)) - alpha q[r]
 template <bool STAGED, int G>
@@ -81,6 +102,9 @@ __device__ void spmv_rows(const BatchDir& d, const float* xs, const float* xg, f
     g.xs = xs;
     g.x = xg;
     const int64_t rows = d.rows;
+    // Thread 0 keeps the L2 `prefetch` row batches ahead of the groups.
+    const int pf = d.prefetch;
+    if (pf > 0 && threadIdx.x == 0) prefetch_rows(d, 0, min(rows, static_cast<int64_t>(pf + 1) * kGroups));
     int64_t r = gid;
     int64_t b = 0, e = 0;
     if (r < rows) {
@@ -88,6 +112,10 @@ __device__ void spmv_rows(const BatchDir& d, const float* xs, const float* xg, f
         e = d.ptr[r + 1];
     }
     for (int64_t r0 = 0; r0 < rows; r0 += kGroups) {
+        if (pf > 0 && threadIdx.x == 0) {
+            const int64_t ra = r0 + static_cast<int64_t>(pf + 1) * kGroups;
+            if (ra < rows) prefetch_rows(d, ra, min(rows, ra + kGroups));
+        }
         const int64_t rn = r + kGroups;
         int64_t nb = 0, ne = 0;
         if (rn < rows) {
@@ -385,7 +413,7 @@ __device__ void solve_problem(const BatchProblem& P, const BatchParams& prm, Bat
             Vj[e] = ((e / w) == (e % w)) ? 1.0 : 0.0;
         }
         __syncthreads();
-        jacobi::jacobi_sweeps(G, w, w, Vj, &ps.flags[0], &ps.flags[1], &ps.flags[2], ps.norms);
+        jacobi::jacobi_sweeps(G, w, w, Vj, &ps.flags[0], &ps.flags[1], &ps.flags[2], ps.norms, ps.pairs);
         sweeps += ps.flags[0];
         jacobi::finish_svd(G, w, w, Vj, ps.BS, BU, w, BV, w, ps.norms, ps.order);
         if (threadIdx.x == 0) {
@@ -487,14 +515,15 @@ __global__ void __launch_bounds__(kBT, 1) batch_pca_kernel(const BatchProblem* _
 // problems it takes, in the given order, and keeps the best time in SM cycles.
 __global__ void __launch_bounds__(kBT, 1) batch_spmv_probe_kernel(const BatchProblem* __restrict__ probs,
                                                                   const int32_t* __restrict__ order, int32_t count,
-                                                                  int32_t adjoint, int32_t group, int32_t reps,
-                                                                  uint64_t* cycles_out) {
+                                                                  int32_t adjoint, int32_t group, int32_t prefetch,
+                                                                  int32_t reps, uint64_t* cycles_out) {
     extern __shared__ __align__(128) unsigned char smem[];
     float* stage = reinterpret_cast<float*>(smem + kPersistBytes);
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         const BatchProblem& P = probs[order[i]];
         BatchDir d = adjoint ? P.adj : P.mul;
         d.group = group;
+        d.prefetch = prefetch;
         float* x = adjoint ? P.Wn : P.xs;
         float* y = adjoint ? P.F : P.Wn;
         for (int64_t c = threadIdx.x; c < d.cols; c += kBT) x[c] = 1.0f;
@@ -539,9 +568,10 @@ void launch_batch_pca(const BatchProblem* probs, const int32_t* order, int32_t c
 }
 
 void launch_batch_spmv_probe(const BatchProblem* probs, const int32_t* order, int32_t count, int32_t adjoint,
-                             int32_t group, int32_t reps, uint64_t* cycles_out, int grid, size_t smem,
-                             cudaStream_t stream) {
-    batch_spmv_probe_kernel<<<grid, kBT, smem, stream>>>(probs, order, count, adjoint, group, reps, cycles_out);
+                             int32_t group, int32_t prefetch, int32_t reps, uint64_t* cycles_out, int grid,
+                             size_t smem, cudaStream_t stream) {
+    batch_spmv_probe_kernel<<<grid, kBT, smem, stream>>>(probs, order, count, adjoint, group, prefetch, reps,
+                                                         cycles_out);
     count_launch();
 }
 

@@ -24,6 +24,7 @@ namespace irlba_gb300 {
 namespace {
 
 constexpr int kCandidates[4] = {4, 8, 16, 32};
+constexpr int kPrefetchCandidates[3] = {0, 1, 3};
 
 // Lanes per row from the average number of 4-entry vectors per row (the
 // schedule used before, or instead of, tuning).
@@ -69,7 +70,7 @@ struct irlba_gb300_batch {
     std::vector<uint8_t> mul_staged, adj_staged;
     int64_t total_nnz = 0, pool_entries = 0, max_staged = 0;
     DevBuf mul_ptr, adj_ptr, mul_val, adj_val, mul_idx16, adj_idx16, mul_idx32, adj_idx32;
-    std::vector<int32_t> g_mul, g_adj;
+    std::vector<int32_t> g_mul, g_adj, pf_mul, pf_adj;
     bool tuned = false, groups_fixed = false;
 
     // Workspace for one (work, number).
@@ -210,8 +211,10 @@ struct irlba_gb300_batch {
         if (!err.empty()) invalid(err);
 
         device_info();
+        // 64 bytes of padding: the kernels' 16-byte-rounded L2 prefetches of the
+        // last rows stay inside the allocation.
         auto up = [](DevBuf& d, const void* h, size_t bytes) {
-            d.alloc(std::max<size_t>(bytes, 16));
+            d.alloc(bytes + 64);
             if (bytes) CUDA_TRY(h2d_sync(d.ptr, h, bytes));
         };
         up(mul_ptr, hp_mul.data(), sizeof(int64_t) * hp_mul.size());
@@ -228,6 +231,8 @@ struct irlba_gb300_batch {
         }
         g_mul.resize(count);
         g_adj.resize(count);
+        pf_mul.assign(count, 1);
+        pf_adj.assign(count, 1);
         for (int j = 0; j < count; ++j) {
             g_mul[j] = heuristic_group(nnz[j], m[j]);
             g_adj[j] = heuristic_group(nnz[j], n[j]);
@@ -251,6 +256,8 @@ struct irlba_gb300_batch {
         if (d.staged) d.idx = (adjoint ? adj_idx16 : mul_idx16).as<uint16_t>() + entry_off[j];
         else d.idx = (adjoint ? adj_idx32 : mul_idx32).as<int32_t>() + entry_off[j];
         d.group = adjoint ? g_adj[j] : g_mul[j];
+        d.prefetch = adjoint ? pf_adj[j] : pf_mul[j];
+        d.idx_bytes = d.staged ? 2 : 4;
         return d;
     }
 
@@ -325,9 +332,10 @@ struct irlba_gb300_batch {
     }
 
     // ---- autotuner ----------------------------------------------------------
-    // Every candidate lane count runs as one probe launch over all active
-    // matrices (so the probe sees the same memory contention as the solve);
-    // each matrix keeps the candidate with its shortest SpMV.
+    // Every candidate schedule (lanes per row x L2 prefetch distance) runs as
+    // one probe launch over all active matrices, so the probe sees the memory
+    // contention of the solve; each matrix and direction keeps the schedule
+    // with its shortest SpMV.
     double tune(int32_t repeats, int32_t active, cudaStream_t s) {
         const auto t0 = std::chrono::steady_clock::now();
         if (active == 0) return 0.0;
@@ -336,18 +344,20 @@ struct irlba_gb300_batch {
         std::vector<uint64_t> best_mul(count, ~0ull), best_adj(count, ~0ull), cyc(count);
         for (int adjoint = 0; adjoint < 2; ++adjoint) {
             for (int g : kCandidates) {
-                launch_batch_spmv_probe(probs_dev.as<BatchProblem>(), order_dev.as<int32_t>(), active, adjoint, g,
-                                        std::max(repeats, 1), cycles_dev.as<uint64_t>(), grid, smem, s);
-                CUDA_TRY(cudaGetLastError());
-                CUDA_TRY(d2h_async(cyc.data(), cycles_dev.ptr, sizeof(uint64_t) * count, s));
-                CUDA_TRY(cudaStreamSynchronize(s));
-                for (int i = 0; i < active; ++i) {
-                    const int j = order[i];
-                    auto& best = adjoint ? best_adj : best_mul;
-                    auto& grp = adjoint ? g_adj : g_mul;
-                    if (cyc[j] < best[j]) {
-                        best[j] = cyc[j];
-                        grp[j] = g;
+                for (int pf : kPrefetchCandidates) {
+                    launch_batch_spmv_probe(probs_dev.as<BatchProblem>(), order_dev.as<int32_t>(), active, adjoint, g,
+                                            pf, std::max(repeats, 1), cycles_dev.as<uint64_t>(), grid, smem, s);
+                    CUDA_TRY(cudaGetLastError());
+                    CUDA_TRY(d2h_async(cyc.data(), cycles_dev.ptr, sizeof(uint64_t) * count, s));
+                    CUDA_TRY(cudaStreamSynchronize(s));
+                    for (int i = 0; i < active; ++i) {
+                        const int j = order[i];
+                        auto& best = adjoint ? best_adj : best_mul;
+                        if (cyc[j] < best[j]) {
+                            best[j] = cyc[j];
+                            (adjoint ? g_adj : g_mul)[j] = g;
+                            (adjoint ? pf_adj : pf_mul)[j] = pf;
+                        }
                     }
                 }
             }
@@ -634,6 +644,8 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
             std::memset(&inf, 0, sizeof(inf));
             inf.group_mul = b->g_mul[j];
             inf.group_adj = b->g_adj[j];
+            inf.prefetch_mul = b->pf_mul[j];
+            inf.prefetch_adj = b->pf_adj[j];
             if (batched[j] && b->results[j].status == 0) {
                 const BatchResult& r = b->results[j];
                 inf.status = IRLBA_GB300_BATCH_OK;

@@ -760,6 +760,11 @@ __global__ void scale_columns_kernel(double* A, int64_t m, int64_t r, const doub
 static void exact_device(const Chain& ch, int64_t requested, double* dU, double* dV, double* dD,
                          cudaStream_t stream) {
     const int64_t m = ch.base->nrow, n = ch.base->ncol;
+    // The one-CTA Jacobi kernel keeps per-column norms and the sort order of
+    // at most 1024 columns in shared memory.
+    if (std::min(m, n) > 1024)
+        throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
+                    "the exact SVD on the device supports a smaller matrix dimension of at most 1024");
     DevBuf dense(sizeof(double) * std::max<int64_t>(m * n, 1));
     realize_device(ch, dense.as<double>(), stream);
     const bool tall = m >= n;

@@ -29,11 +29,21 @@ static __device__ __forceinline__ int circle_partner_b(int round, int slot, int 
 }
 
 // One-sided Jacobi on G (m x n, column-major, ld m) accumulating V (n x n, ld n).
-// Whole CTA participates. Returns the number of sweeps in *sweeps.
+// Whole CTA participates. Each round runs in three phases separated by CTA
+// barriers: (1) one warp per column pair forms the dot product g_pq; (2) one
+// thread per pair derives the rotation from g_pq and the column norms, so the
+// long FP64 divide/square-root sequences run once per 32 pairs instead of
+// once per warp; (3) one warp per pair rotates the two columns of G and V.
+// pairs: >= 3 * ((n + 1) / 2) doubles of scratch (shared memory).
+// Returns the number of sweeps in *sweeps.
 static __device__ void jacobi_sweeps(double* G, int64_t m, int n, double* V, int* sweeps, int* not_converged,
-                              int* rotated_flag, double* nrm) {
+                                     int* rotated_flag, double* nrm, double* pairs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int n2 = n + (n & 1);
+    const int half = n2 / 2;
+    double* pg = pairs;
+    double* pc = pairs + half;
+    double* ps = pairs + 2 * half;
     const double eps = 2.220446049250313e-16;
     const double thresh = eps * static_cast<double>(m);
     int sweep = 0;
@@ -49,7 +59,7 @@ static __device__ void jacobi_sweeps(double* G, int64_t m, int n, double* V, int
         if (threadIdx.x == 0) *rotated_flag = 0;
         __syncthreads();
         for (int round = 0; round < n2 - 1; ++round) {
-            for (int slot = warp; slot < n2 / 2; slot += nw) {
+            for (int slot = warp; slot < half; slot += nw) {
                 int p = circle_partner_a(round, slot, n2);
                 int q = circle_partner_b(round, slot, n2);
                 if (p > q) {
@@ -58,39 +68,66 @@ static __device__ void jacobi_sweeps(double* G, int64_t m, int n, double* V, int
                     q = tmp;
                 }
                 if (q >= n) continue;
-                double* gp = G + p * m;
-                double* gq = G + q * m;
+                const double* gp = G + p * m;
+                const double* gq = G + q * m;
                 double g = 0;
                 for (int64_t i = lane; i < m; i += 32) g += gp[i] * gq[i];
                 g = warp_sum(g);
-                const double a = nrm[p], b = nrm[q];
-                if (g == 0.0 || fabs(g) <= thresh * sqrt(a * b)) continue;
-                // Rotation parameters once per pair (lane 0), then broadcast:
-                // FP64 sqrt and division are long multi-instruction sequences.
-                double c = 0, s = 0, t = 0;
-                if (lane == 0) {
-                    const double zeta = (b - a) / (2.0 * g);
-                    t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                    c = 1.0 / sqrt(1.0 + t * t);
-                    s = c * t;
-                    nrm[p] = a - t * g;
-                    nrm[q] = b + t * g;
+                if (lane == 0) pg[slot] = g;
+            }
+            __syncthreads();
+            // Rotation parameters (c = 0 marks a pair left alone).
+            for (int slot = threadIdx.x; slot < half; slot += blockDim.x) {
+                int p = circle_partner_a(round, slot, n2);
+                int q = circle_partner_b(round, slot, n2);
+                if (p > q) {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
                 }
-                c = __shfl_sync(0xffffffffu, c, 0);
-                s = __shfl_sync(0xffffffffu, s, 0);
+                double c = 0, sn = 0;
+                if (q < n) {
+                    const double g = pg[slot];
+                    const double a = nrm[p], b = nrm[q];
+                    if (!(g == 0.0 || fabs(g) <= thresh * sqrt(a * b))) {
+                        const double zeta = (b - a) / (2.0 * g);
+                        const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                        c = 1.0 / sqrt(1.0 + t * t);
+                        sn = c * t;
+                        nrm[p] = a - t * g;
+                        nrm[q] = b + t * g;
+                        *rotated_flag = 1;
+                    }
+                }
+                pc[slot] = c;
+                ps[slot] = sn;
+            }
+            __syncthreads();
+            for (int slot = warp; slot < half; slot += nw) {
+                const double c = pc[slot];
+                if (c == 0.0) continue;
+                const double sn = ps[slot];
+                int p = circle_partner_a(round, slot, n2);
+                int q = circle_partner_b(round, slot, n2);
+                if (p > q) {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                double* gp = G + p * m;
+                double* gq = G + q * m;
                 for (int64_t i = lane; i < m; i += 32) {
                     const double x = gp[i], y = gq[i];
-                    gp[i] = c * x - s * y;
-                    gq[i] = s * x + c * y;
+                    gp[i] = c * x - sn * y;
+                    gq[i] = sn * x + c * y;
                 }
                 double* vp = V + p * n;
                 double* vq = V + q * n;
                 for (int i = lane; i < n; i += 32) {
                     const double x = vp[i], y = vq[i];
-                    vp[i] = c * x - s * y;
-                    vq[i] = s * x + c * y;
+                    vp[i] = c * x - sn * y;
+                    vq[i] = sn * x + c * y;
                 }
-                if (lane == 0) *rotated_flag = 1;
             }
             __syncthreads();
         }

@@ -167,6 +167,8 @@ struct BatchDir {
     const float* val = nullptr;
     int32_t staged = 0;                // gathered vector copied to shared memory
     int32_t group = 32;                // lanes per row: 4, 8, 16 or 32
+    int32_t prefetch = 0;              // row batches bulk-prefetched into L2 ahead (0 = off)
+    int32_t idx_bytes = 2;             // 2 (u16, staged) or 4 (int32)
 };
 
 struct BatchProblem {
@@ -256,10 +258,11 @@ cudaError_t batch_configure(size_t max_smem_optin);
 void launch_batch_pca(const BatchProblem* probs, const int32_t* order, int32_t count, const BatchParams& prm,
                       BatchResult* results, uint32_t* queue, int grid, size_t smem, cudaStream_t stream);
 // Autotuner probe: CTAs take the problems in `order` and time `reps` SpMVs of
-// each (direction adjoint, `group` lanes per row), writing the best time in SM
-// cycles to cycles_out[problem]. Uses the problems' xs/Wn/F as scratch.
+// each (direction adjoint, `group` lanes per row, `prefetch` row batches of L2
+// prefetch), writing the best time in SM cycles to cycles_out[problem]. Uses
+// the problems' xs/Wn/F as scratch.
 void launch_batch_spmv_probe(const BatchProblem* probs, const int32_t* order, int32_t count, int32_t adjoint,
-                             int32_t group, int32_t reps, uint64_t* cycles_out, int grid, size_t smem,
-                             cudaStream_t stream);
+                             int32_t group, int32_t prefetch, int32_t reps, uint64_t* cycles_out, int grid,
+                             size_t smem, cudaStream_t stream);
 
 }  // namespace irlba_gb300

@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(kSvdThreads) restart_kernel(RestartArgs a, int
     extern __shared__ __align__(16) double sm[];
     __shared__ double norms[1024];
     __shared__ int order[1024];
+    __shared__ double pairs[3 * 64];
     __shared__ int rotated;
     __shared__ int sweeps, notconv;
     Ctrl* ctrl = a.ctrl;
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(kSvdThreads) restart_kernel(RestartArgs a, int
         V[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
     }
     __syncthreads();
-    jacobi_sweeps(G, n, n, V, &sweeps, &notconv, &rotated, norms);
+    jacobi_sweeps(G, n, n, V, &sweeps, &notconv, &rotated, norms, pairs);
     finish_svd(G, n, n, V, a.BS, a.BU, n, a.BV, n, norms, order);
     restart_tail(a, sweeps, notconv);
 }
@@ -106,8 +107,10 @@ __global__ void __launch_bounds__(kSvdThreads) restart_kernel(RestartArgs a, int
 // operations per clock per SM, so one SM runs a 57 x 57 Jacobi sweep in about
 // half a millisecond. The cluster keeps G and V in CTA 0's shared memory and
 // gives each of its warps one column pair per round through distributed shared
-// memory; rounds are separated by cluster barriers. The arithmetic is the same
-// as the single-CTA form (same ordering, same formulas).
+// memory; rounds are separated by cluster barriers. Within a CTA the rotation
+// parameters of its warps' pairs are derived by one thread each, in parallel
+// lanes. The arithmetic is the same as the single-CTA form (same ordering,
+// same formulas).
 // ---------------------------------------------------------------------------
 constexpr int kClusterCTAs = 8;
 constexpr int kClusterThreads = 128;
@@ -121,6 +124,8 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kClusterT
     __shared__ double norms_local[kClusterMaxRows];
     __shared__ int order[kClusterMaxRows];
     __shared__ int rotated_local;
+    __shared__ double pair_g[kClusterThreads / 32], pair_c[kClusterThreads / 32], pair_s[kClusterThreads / 32];
+    __shared__ int pair_p[kClusterThreads / 32], pair_q[kClusterThreads / 32];
     const unsigned rank = cl.block_rank();
     const int n = a.work;
     const int nn = n * n;
@@ -158,54 +163,84 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kClusterT
         if (rank == 0 && threadIdx.x == 0) *rotated = 0;
         cl.sync();
         for (int round = 0; round < n2 - 1; ++round) {
-            for (int slot = gw; slot < n2 / 2; slot += gnw) {
-                int p = circle_partner_a(round, slot, n2);
-                int q = circle_partner_b(round, slot, n2);
-                if (p > q) {
-                    const int tmp = p;
-                    p = q;
-                    q = tmp;
+            // Slots are taken gnw at a time so every thread runs the same
+            // number of phases. Phase 1: each warp caches its two columns and
+            // forms g; phase 2: one thread per local warp derives the rotation
+            // (the FP64 divides and square roots run in parallel lanes of one
+            // warp, not once per warp); phase 3: the warps rotate.
+            for (int base = 0; base < n2 / 2; base += gnw) {
+                const int slot = base + gw;
+                int p = 0, q = n;
+                if (slot < n2 / 2) {
+                    p = circle_partner_a(round, slot, n2);
+                    q = circle_partner_b(round, slot, n2);
+                    if (p > q) {
+                        const int tmp = p;
+                        p = q;
+                        q = tmp;
+                    }
                 }
-                if (q >= n) continue;
+                const bool live = q < n;
                 double* gp = G + p * n;
                 double* gq = G + q * n;
                 double xp[kClusterMaxRows / 32], xq[kClusterMaxRows / 32];
-                double g = 0;
+                if (live) {
+                    double g = 0;
 #pragma unroll
-                for (int u = 0; u < kClusterMaxRows / 32; ++u) {
-                    const int i = lane + 32 * u;
-                    xp[u] = i < n ? gp[i] : 0.0;
-                    xq[u] = i < n ? gq[i] : 0.0;
-                    g += xp[u] * xq[u];
+                    for (int u = 0; u < kClusterMaxRows / 32; ++u) {
+                        const int i = lane + 32 * u;
+                        xp[u] = i < n ? gp[i] : 0.0;
+                        xq[u] = i < n ? gq[i] : 0.0;
+                        g += xp[u] * xq[u];
+                    }
+                    g = warp_sum(g);
+                    if (lane == 0) {
+                        pair_g[warp] = g;
+                        pair_p[warp] = p;
+                        pair_q[warp] = q;
+                    }
+                } else if (lane == 0) {
+                    pair_q[warp] = n;
                 }
-                g = warp_sum(g);
-                const double av = nrm[p], bv = nrm[q];
-                if (g == 0.0 || fabs(g) <= thresh * sqrt(av * bv)) continue;
-                double c = 0, s = 0;
-                if (lane == 0) {
-                    const double zeta = (bv - av) / (2.0 * g);
-                    const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                    c = 1.0 / sqrt(1.0 + t * t);
-                    s = c * t;
-                    nrm[p] = av - t * g;
-                    nrm[q] = bv + t * g;
-                    *rotated = 1;
+                __syncthreads();
+                if (threadIdx.x < nw) {
+                    const int t = threadIdx.x;
+                    double c = 0, sn = 0;
+                    if (pair_q[t] < n) {
+                        const int pp = pair_p[t], qq = pair_q[t];
+                        const double g = pair_g[t];
+                        const double av = nrm[pp], bv = nrm[qq];
+                        if (!(g == 0.0 || fabs(g) <= thresh * sqrt(av * bv))) {
+                            const double zeta = (bv - av) / (2.0 * g);
+                            const double tt = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                            c = 1.0 / sqrt(1.0 + tt * tt);
+                            sn = c * tt;
+                            nrm[pp] = av - tt * g;
+                            nrm[qq] = bv + tt * g;
+                            *rotated = 1;
+                        }
+                    }
+                    pair_c[t] = c;
+                    pair_s[t] = sn;
                 }
-                c = __shfl_sync(0xffffffffu, c, 0);
-                s = __shfl_sync(0xffffffffu, s, 0);
-                double* vp = V + p * n;
-                double* vq = V + q * n;
+                __syncthreads();
+                const double c = pair_c[warp], sn = pair_s[warp];
+                if (live && c != 0.0) {
+                    double* vp = V + p * n;
+                    double* vq = V + q * n;
 #pragma unroll
-                for (int u = 0; u < kClusterMaxRows / 32; ++u) {
-                    const int i = lane + 32 * u;
-                    if (i < n) {
-                        gp[i] = c * xp[u] - s * xq[u];
-                        gq[i] = s * xp[u] + c * xq[u];
-                        const double y = vp[i], z = vq[i];
-                        vp[i] = c * y - s * z;
-                        vq[i] = s * y + c * z;
+                    for (int u = 0; u < kClusterMaxRows / 32; ++u) {
+                        const int i = lane + 32 * u;
+                        if (i < n) {
+                            gp[i] = c * xp[u] - sn * xq[u];
+                            gq[i] = sn * xp[u] + c * xq[u];
+                            const double y = vp[i], z = vq[i];
+                            vp[i] = c * y - sn * z;
+                            vq[i] = sn * y + c * z;
+                        }
                     }
                 }
+                __syncthreads();
             }
             cl.sync();
         }
@@ -224,6 +259,7 @@ __global__ void __launch_bounds__(kSvdThreads) dense_svd_kernel(const double* A,
                                                                  double* V, double* scratch, Ctrl* ctrl) {
     __shared__ double norms[1024];
     __shared__ int order[1024];
+    __shared__ double pairs[3 * 512];
     __shared__ int rotated;
     __shared__ int sweeps, notconv;
     double* G = scratch;
@@ -231,7 +267,7 @@ __global__ void __launch_bounds__(kSvdThreads) dense_svd_kernel(const double* A,
     for (int64_t e = threadIdx.x; e < m * n; e += blockDim.x) G[e] = A[e];
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) VV[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
     __syncthreads();
-    jacobi_sweeps(G, m, n, VV, &sweeps, &notconv, &rotated, norms);
+    jacobi_sweeps(G, m, n, VV, &sweeps, &notconv, &rotated, norms, pairs);
     finish_svd(G, m, n, VV, S, U, m, V, n, norms, order);
     if (threadIdx.x == 0 && ctrl) {
         ctrl->svd_sweeps = sweeps;

@@ -279,7 +279,10 @@ typedef struct {
     int32_t iterations;      /* restart iterations, as Results::iterations */
     int32_t group_mul;       /* lanes per row of the multiply SpMV */
     int32_t group_adj;       /* lanes per row of the adjoint SpMV */
+    int32_t prefetch_mul;    /* row batches prefetched into L2 ahead, multiply */
+    int32_t prefetch_adj;    /* same, adjoint */
     int32_t error;           /* irlba_gb300_status of a failed single-matrix solve */
+    int32_t reserved0;
     int64_t lanczos_steps;
     int64_t svd_sweeps;
     double ms;               /* device time of this matrix on its CTA */
@@ -307,7 +310,8 @@ irlba_gb300_status irlba_gb300_batch_create(int32_t count, const int64_t* nrow, 
 irlba_gb300_status irlba_gb300_batch_destroy(irlba_gb300_batch* batch);
 
 /* Runs the autotuner now (otherwise the first solve does): `repeats` timed
- * SpMVs per candidate and direction. */
+ * SpMVs per candidate schedule (lanes per row 4/8/16/32 x L2 prefetch
+ * distance 0/1/3 row batches) and direction. */
 irlba_gb300_status irlba_gb300_batch_tune(irlba_gb300_batch* batch, int32_t repeats, void* stream);
 /* Lanes per row chosen for each matrix (arrays of `count`, either may be NULL). */
 irlba_gb300_status irlba_gb300_batch_groups(const irlba_gb300_batch* batch, int32_t* group_mul,
