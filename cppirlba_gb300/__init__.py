@@ -92,6 +92,8 @@ class BatchStats(ctypes.Structure):
         ("graph_captured", ctypes.c_int32),
         ("single", ctypes.c_int32),
         ("ctas", ctypes.c_int32),
+        ("team", ctypes.c_int32),
+        ("joint", ctypes.c_int32),
         ("reserved0", ctypes.c_int32),
         ("nnz", ctypes.c_int64),
         ("lanczos_steps", ctypes.c_int64),
@@ -151,6 +153,7 @@ def load_library():
         "irlba_gb300_batch_create": (i32, [i32, P, P, P, i32, P, P, i32, ctypes.POINTER(P)]),
         "irlba_gb300_batch_destroy": (i32, [P]),
         "irlba_gb300_batch_tune": (i32, [P, i32, P]),
+        "irlba_gb300_batch_set_team": (i32, [P, i32, i32]),
         "irlba_gb300_batch_groups": (i32, [P, P, P]),
         "irlba_gb300_batch_set_groups": (i32, [P, P, P]),
         "irlba_gb300_batch_pca": (i32, [P, i32, i32, i64, ctypes.POINTER(_Options), ctypes.POINTER(BatchStats), P]),
@@ -521,6 +524,11 @@ class Batch:
         ga = None if group_adj is None else np.ascontiguousarray(group_adj, dtype=np.int32)
         _check(load_library().irlba_gb300_batch_set_groups(self._h, None if gm is None else _vptr(gm),
                                                            None if ga is None else _vptr(ga)))
+
+    def set_team(self, team, joint=-1):
+        """CTAs per team (1, 2, 4; 0 = automatic) and how many of the largest
+        matrices a team solves together (-1 = automatic)."""
+        _check(load_library().irlba_gb300_batch_set_team(self._h, int(team), int(joint)))
 
     def tune(self, repeats=3, stream=None):
         _check(load_library().irlba_gb300_batch_tune(self._h, repeats, stream))

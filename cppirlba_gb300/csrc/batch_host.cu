@@ -84,12 +84,20 @@ struct irlba_gb300_batch {
     std::vector<irlba_gb300_batch_info> info;
     int64_t last_number = 0;
     int32_t last_center = 0, last_scale = 0;
+    // Start vectors in the workspace: for which workspace and seed.
+    uint64_t init_gen = ~0ull, init_seed = 0;
+    bool init_random = false;
     bool have_results = false;
+
+    // CTAs per team (0 = chosen per call from the cost estimate) and the number
+    // of largest matrices a team solves jointly (-1 = from the cost estimate).
+    int team_request = 0;
+    int joint_request = -1;
 
     // Graph of [queue reset, persistent kernel] for one parameter set.
     cudaGraphExec_t exec = nullptr;
     BatchParams graph_prm;
-    int graph_grid = 0, graph_count = 0;
+    int graph_grid = 0, graph_count = 0, graph_team = 0, graph_joint = 0;
     size_t graph_smem = 0;
     uint64_t graph_gen = 0, ws_gen = 0;
 
@@ -317,6 +325,16 @@ struct irlba_gb300_batch {
         ++ws_gen;
     }
 
+    // Descriptors on the device are rebuilt when the workspace or a schedule changes.
+    uint64_t sched_version = 1, uploaded_ws_gen = ~0ull, uploaded_sched = 0;
+
+    void upload_problems_if_changed(cudaStream_t s) {
+        if (uploaded_ws_gen == ws_gen && uploaded_sched == sched_version) return;
+        upload_problems(s);
+        uploaded_ws_gen = ws_gen;
+        uploaded_sched = sched_version;
+    }
+
     void upload_problems(cudaStream_t s) {
         for (int j = 0; j < count; ++j) {
             probs[j].mul = dir(j, false);
@@ -329,6 +347,57 @@ struct irlba_gb300_batch {
     int grid_for(int32_t active) const {
         const DeviceInfo& di = device_info();
         return std::max(1, std::min<int>(active, di.sms));
+    }
+
+    // Team size and joint prefix for the active matrices (in cost order). A
+    // matrix is solved by a whole team when its cost exceeds half of the
+    // average per-CTA load; the rest run one per CTA. The candidate (1, 2 or 4
+    // CTAs per team) with the smallest estimated makespan
+    //   max(largest cost / (team * eff), (joint cost / eff + solo cost) / CTAs)
+    // wins; eff (1, 0.9, 0.8) charges the team barriers.
+    int choose_team(int32_t active, const std::vector<int64_t>& cost, size_t smem, int* teams_out,
+                    int* joint_out) const {
+        int best = 1, best_teams = 1, best_joint = 0;
+        double best_est = 1e300;
+        const int cands[3] = {1, 2, 4};
+        const double eff[3] = {1.0, 0.9, 0.8};
+        int64_t mx = 0, tot = 0;
+        for (int i = 0; i < active; ++i) {
+            mx = std::max(mx, cost[order[i]]);
+            tot += cost[order[i]];
+        }
+        for (int c = 0; c < 3; ++c) {
+            if (team_request && cands[c] != team_request) continue;
+            const int resident = batch_max_teams(cands[c], smem);
+            if (resident < 1) continue;
+            const int teams = std::min(resident, std::max(active, 1));
+            const double ctas = static_cast<double>(teams) * cands[c];
+            int joint = 0;
+            double joint_cost = 0, solo_cost = 0;
+            for (int i = 0; i < active; ++i) {
+                const double cj = static_cast<double>(cost[order[i]]);
+                const bool take = joint_request >= 0 ? i < joint_request : cj > 0.5 * tot / ctas;
+                if (cands[c] > 1 && joint == i && take) {
+                    ++joint;
+                    joint_cost += cj;
+                } else {
+                    solo_cost += cj;
+                }
+            }
+            const double largest = joint > 0 ? mx / (cands[c] * eff[c]) : static_cast<double>(mx);
+            const double est = std::max(largest, (joint_cost / eff[c] + solo_cost) / ctas);
+            if (est < best_est) {
+                best_est = est;
+                best = cands[c];
+                best_teams = teams;
+                best_joint = joint;
+            }
+        }
+        if (best_est == 1e300)
+            throw Error(IRLBA_GB300_ERROR_CUDA, "no team size of the batched kernel can be resident on this device");
+        *teams_out = best_teams;
+        *joint_out = best > 1 ? best_joint : active;
+        return best;
     }
 
     // ---- autotuner ----------------------------------------------------------
@@ -363,6 +432,7 @@ struct irlba_gb300_batch {
             }
         }
         tuned = true;
+        ++sched_version;
         return ms_since(t0);
     }
 };
@@ -484,6 +554,7 @@ irlba_gb300_status irlba_gb300_batch_set_groups(irlba_gb300_batch* batch, const 
         check(group_adj);
         if (group_mul) std::copy(group_mul, group_mul + batch->count, batch->g_mul.begin());
         if (group_adj) std::copy(group_adj, group_adj + batch->count, batch->g_adj.begin());
+        ++batch->sched_version;
         batch->groups_fixed = true;
         batch->tuned = true;
     });
@@ -533,10 +604,10 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
         b->workspace(w32, number);
 
         // Start vectors: the same options give every matrix the vector that a
-        // separate pca() call would draw (compute.hpp:179-190).
-        {
+        // separate pca() call would draw (compute.hpp:179-190). Uploaded when
+        // the workspace, the seed or the caller's initial vector changes.
+        if (opt.initial || b->init_gen != b->ws_gen || b->init_seed != opt.seed || !b->init_random) {
             std::map<int64_t, std::vector<double>> by_n;
-            std::vector<double> host(b->ws64.bytes / sizeof(double), 0.0);
             bool any = false;
             for (int j = 0; j < count; ++j) {
                 if (!batched[j]) continue;
@@ -552,12 +623,13 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
                     }
                     it = by_n.emplace(b->n[j], std::move(v)).first;
                 }
-                const int64_t off = b->probs[j].init - b->ws64.as<double>();
-                std::copy(it->second.begin(), it->second.end(), host.begin() + off);
-                CUDA_TRY(h2d_async(const_cast<double*>(b->probs[j].init), host.data() + off,
+                CUDA_TRY(h2d_async(const_cast<double*>(b->probs[j].init), it->second.data(),
                                    sizeof(double) * b->n[j], s));
             }
             if (any) CUDA_TRY(cudaStreamSynchronize(s));
+            b->init_gen = b->ws_gen;
+            b->init_seed = opt.seed;
+            b->init_random = opt.initial == nullptr;
         }
 
         // Largest first (longest-processing-time order): cost ~ stored entries
@@ -565,16 +637,17 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
         b->order.clear();
         for (int j = 0; j < count; ++j)
             if (batched[j]) b->order.push_back(j);
-        auto cost = [&](int j) { return 2 * b->nnz[j] + (b->m[j] + b->n[j]) * static_cast<int64_t>(w32) * 4; };
-        std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+        std::vector<int64_t> costs(count);
+        for (int j = 0; j < count; ++j) costs[j] = 2 * b->nnz[j] + (b->m[j] + b->n[j]) * static_cast<int64_t>(w32) * 4;
+        std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return costs[x] > costs[y]; });
         const int32_t active = static_cast<int32_t>(b->order.size());
         if (active) CUDA_TRY(h2d_async(b->order_dev.ptr, b->order.data(), sizeof(int32_t) * active, s));
-        b->upload_problems(s);
+        b->upload_problems_if_changed(s);
 
         double tune_ms = 0;
         if (!b->tuned && active) {
             tune_ms = b->tune(3, active, s);
-            b->upload_problems(s);
+            b->upload_problems_if_changed(s);
         }
 
         BatchParams prm;
@@ -589,12 +662,15 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
         prm.eps = opt.invariant_subspace_tolerance < 0 ? std::pow(std::numeric_limits<double>::epsilon(), 0.8)
                                                        : opt.invariant_subspace_tolerance;
         const size_t smem = batch_smem_bytes(b->max_staged);
-        const int grid = b->grid_for(active);
+        int teams = 1, n_joint = 0;
+        const int team = active ? b->choose_team(active, costs, smem, &teams, &n_joint) : 1;
+        const int grid = teams * team;
         int captured = 0;
         float dev_ms = 0;
         if (active) {
             const bool same = b->exec && b->graph_gen == b->ws_gen && b->graph_grid == grid &&
-                              b->graph_smem == smem && b->graph_count == active &&
+                              b->graph_team == team && b->graph_joint == n_joint && b->graph_smem == smem &&
+                              b->graph_count == active &&
                               std::memcmp(&b->graph_prm, &prm, sizeof(prm)) == 0;
             if (!same) {
                 if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -605,8 +681,9 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
                 cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
                 if (e == cudaSuccess) {
                     cudaMemsetAsync(b->queue_dev.ptr, 0, sizeof(uint32_t), cs);
-                    launch_batch_pca(b->probs_dev.as<BatchProblem>(), b->order_dev.as<int32_t>(), active, prm,
-                                     b->results_dev.as<BatchResult>(), b->queue_dev.as<uint32_t>(), grid, smem, cs);
+                    launch_batch_pca(team, b->probs_dev.as<BatchProblem>(), b->order_dev.as<int32_t>(), active,
+                                     n_joint, prm, b->results_dev.as<BatchResult>(), b->queue_dev.as<uint32_t>(),
+                                     teams, smem, cs);
                     e = cudaStreamEndCapture(cs, &graph);
                 }
                 if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, graph, 0);
@@ -615,6 +692,8 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
                 CUDA_TRY(e);
                 b->graph_prm = prm;
                 b->graph_grid = grid;
+                b->graph_team = team;
+                b->graph_joint = n_joint;
                 b->graph_smem = smem;
                 b->graph_count = active;
                 b->graph_gen = b->ws_gen;
@@ -674,10 +753,21 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
             stats->graph_captured = captured;
             stats->single = single;
             stats->ctas = active ? grid : 0;
+            stats->team = active ? team : 0;
+            stats->joint = active ? n_joint : 0;
             stats->nnz = b->total_nnz;
             stats->lanczos_steps = steps;
         }
         (void)t_call;
+    });
+}
+
+irlba_gb300_status irlba_gb300_batch_set_team(irlba_gb300_batch* b, int32_t team, int32_t joint) {
+    return guarded([&]() {
+        if (!b) invalid("batch is NULL");
+        if (team != 0 && team != 1 && team != 2 && team != 4) invalid("team must be 0 (automatic), 1, 2 or 4");
+        b->team_request = team;
+        b->joint_request = joint < 0 ? -1 : joint;
     });
 }
 
@@ -688,9 +778,9 @@ irlba_gb300_status irlba_gb300_batch_tune(irlba_gb300_batch* b, int32_t repeats,
         StreamScope ss(stream);
         b->tuned = false;
         b->groups_fixed = false;
-        b->upload_problems(ss.s);
+        b->upload_problems_if_changed(ss.s);
         b->tune(repeats, static_cast<int32_t>(b->order.size()), ss.s);
-        b->upload_problems(ss.s);
+        b->upload_problems_if_changed(ss.s);
     });
 }
 

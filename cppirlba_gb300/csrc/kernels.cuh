@@ -155,7 +155,7 @@ void launch_dense_svd(const double* A, int64_t m, int64_t n, double* U, double* 
 
 // ---------------------------------------------------------------------------
 // Batched form (batch.cu): one persistent launch solves many independent
-// centred/scaled sparse PCAs in the FP32 form, one CTA per problem.
+// centred/scaled sparse PCAs in the FP32 form, one team of CTAs per problem.
 // ---------------------------------------------------------------------------
 // One gather direction of one problem: plain CSR over `rows` output entries.
 // Row 0 of ptr starts at a multiple of 4 entries (16-byte aligned values).
@@ -255,8 +255,14 @@ int64_t batch_stage_limit();
 // Dynamic shared memory of the batched kernels for a given largest staged vector.
 size_t batch_smem_bytes(int64_t max_staged);
 cudaError_t batch_configure(size_t max_smem_optin);
-void launch_batch_pca(const BatchProblem* probs, const int32_t* order, int32_t count, const BatchParams& prm,
-                      BatchResult* results, uint32_t* queue, int grid, size_t smem, cudaStream_t stream);
+// Teams of `team` CTAs (a thread-block cluster; 1, 2 or 4) that can be
+// resident at once with `smem` bytes of dynamic shared memory (0 on error).
+int batch_max_teams(int team, size_t smem);
+// `teams` teams of `team` CTAs take the `count` problems of `order` in turn:
+// the first n_joint each by a whole team, the rest one CTA each.
+void launch_batch_pca(int team, const BatchProblem* probs, const int32_t* order, int32_t count, int32_t n_joint,
+                      const BatchParams& prm, BatchResult* results, uint32_t* queue, int teams, size_t smem,
+                      cudaStream_t stream);
 // Autotuner probe: CTAs take the problems in `order` and time `reps` SpMVs of
 // each (direction adjoint, `group` lanes per row, `prefetch` row batches of L2
 // prefetch), writing the best time in SM cycles to cycles_out[problem]. Uses

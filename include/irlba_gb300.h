@@ -259,8 +259,10 @@ irlba_gb300_status irlba_gb300_svd_adjoint_sparse(const irlba_gb300_matrix* matr
  * loop of irlba::pca(matrix_j, center, scale, number, options) would, in one
  * persistent kernel launch replayed from a captured CUDA graph (one CTA per
  * matrix, largest first; FP32 matrices and bases with FP64 recurrence, small
- * SVD and convergence test). The gather schedule of each matrix's SpMVs (lanes
- * per row) is picked by an autotuner that times the candidates on the device.
+ * SVD and convergence test). Large matrices are shared by a team of CTAs (a
+ * thread-block cluster). The gather schedule of each matrix's SpMVs (lanes per
+ * row, L2 prefetch distance) is picked by an autotuner that times the
+ * candidates on the device.
  * Matrices whose iterations hit an invariant subspace, or whose arguments need
  * the exact SVD or a working subspace above 32, are solved by the
  * single-matrix FP32 form instead (status IRLBA_GB300_BATCH_SINGLE).
@@ -296,6 +298,8 @@ typedef struct {
     int32_t graph_captured;  /* 1 if this call captured a new graph */
     int32_t single;          /* matrices solved by the single-matrix engine */
     int32_t ctas;            /* CTAs of the persistent launch */
+    int32_t team;            /* CTAs per team (a thread-block cluster) */
+    int32_t joint;           /* matrices solved by a whole team */
     int32_t reserved0;
     int64_t nnz;             /* stored entries over all matrices (one direction) */
     int64_t lanczos_steps;   /* summed over the batched matrices */
@@ -313,6 +317,12 @@ irlba_gb300_status irlba_gb300_batch_destroy(irlba_gb300_batch* batch);
  * SpMVs per candidate schedule (lanes per row 4/8/16/32 x L2 prefetch
  * distance 0/1/3 row batches) and direction. */
 irlba_gb300_status irlba_gb300_batch_tune(irlba_gb300_batch* batch, int32_t repeats, void* stream);
+/* Teams of CTAs (thread-block clusters of `team` = 1, 2 or 4 CTAs; 0, the
+ * default, picks per call the size with the smallest estimated makespan). A
+ * team solves each of the `joint` largest matrices together and the others
+ * one matrix per CTA; joint < 0 (default) picks the matrices whose cost
+ * exceeds half of the average per-CTA load. */
+irlba_gb300_status irlba_gb300_batch_set_team(irlba_gb300_batch* batch, int32_t team, int32_t joint);
 /* Lanes per row chosen for each matrix (arrays of `count`, either may be NULL). */
 irlba_gb300_status irlba_gb300_batch_groups(const irlba_gb300_batch* batch, int32_t* group_mul,
                                             int32_t* group_adj);

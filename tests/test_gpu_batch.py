@@ -48,7 +48,7 @@ def test_batch_matches_oracle(engine, oracle_mod, center, scale):
     init = np.random.default_rng(7).standard_normal(genes)
     b = _batch(engine, inputs)
     st = b.pca(center, scale, 6, engine.Options(initial=init))
-    assert st["single"] == 0 and st["ctas"] == len(sizes)
+    assert st["single"] == 0 and st["team"] in (1, 2, 4) and st["ctas"] % st["team"] == 0
     for j, x in enumerate(inputs):
         res = b.result(j)
         assert res.stats["status"] == engine.BATCH_OK
@@ -59,6 +59,32 @@ def test_batch_matches_oracle(engine, oracle_mod, center, scale):
             np.testing.assert_allclose(res.center, orc["center"], rtol=1e-12, atol=1e-15)
         if scale:
             np.testing.assert_allclose(res.scale, orc["scale"], rtol=1e-12)
+    b.close()
+
+
+@pytest.mark.parametrize("team,joint", [(1, -1), (2, 5), (4, 5), (4, 2), (4, 0)])
+def test_batch_team_sizes(engine, oracle_mod, team, joint):
+    """Every team size (CTAs per team, a thread-block cluster), with all, some
+    or none of the matrices solved jointly, gives the oracle's results, down to
+    matrices of a few dozen cells split over the team."""
+    sizes = [3100, 40, 640, 25, 1800]
+    genes = 180
+    inputs = _inputs(sizes, genes, seed=47)
+    init = np.random.default_rng(8).standard_normal(genes)
+    b = _batch(engine, inputs)
+    b.set_team(team, joint)
+    st = b.pca(True, True, 3, engine.Options(initial=init))
+    assert st["team"] == team and st["ctas"] % team == 0
+    if team > 1:
+        assert st["joint"] == joint
+    for j, x in enumerate(inputs):
+        res = b.result(j)
+        orc = _oracle(oracle_mod, x, True, True, 3, init)
+        if res.stats["status"] == engine.BATCH_OK:
+            _close(res, orc)
+        else:
+            assert res.stats["status"] == engine.BATCH_SINGLE
+            _close(res, orc, var_tol=1e-4)
     b.close()
 
 
