@@ -23,6 +23,7 @@
 #include <string>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "host.hpp"
@@ -338,6 +339,13 @@ struct Engine {
     DevBuf center_d, scale_d;
     Ctrl* ctrl = nullptr;
 
+    // FP32 form: the first product of the next Lanczos run, A'(F / ||F||) =
+    // (A'F) / ||F||, is formed on a side stream while the restart kernel runs
+    // (it needs F, not the small SVD). pre_ready: Wn holds A'F.
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_f = nullptr, ev_pre = nullptr;
+    bool pre_ready = false;
+
     // Chain vectors in T precision.
     const T* cvec = nullptr;   // centre (length n)
     const T* svec = nullptr;   // scale (length n or m)
@@ -345,6 +353,14 @@ struct Engine {
     Engine(const Chain& c, cudaStream_t s) : ch(c), A(*c.base), stream(s), m(c.base->nrow), n(c.base->ncol) {
         timer.stream = s;
         timer.on = g_profile;
+    }
+    ~Engine() {
+        if (side) {
+            cudaStreamSynchronize(side);
+            cudaStreamDestroy(side);
+        }
+        if (ev_f) cudaEventDestroy(ev_f);
+        if (ev_pre) cudaEventDestroy(ev_pre);
     }
 
     void upload_chain() {
@@ -378,8 +394,13 @@ struct Engine {
 
     // ---- the fused matvecs ----------------------------------------------------
     // multiply: y (m) = Op x (n).  beta_mul must already hold the centring scalar.
-    void multiply(const T* x, T* y, const double* alpha, const T* q) {
-        Scoped sc(timer, kTSpmvMul);
+    // st: the stream (NULL = the engine stream).
+    void multiply(const T* x, T* y, const double* alpha, const T* q, cudaStream_t st = nullptr) {
+        const cudaStream_t ms = st ? st : stream;
+        // The per-class timer records on the engine stream: side-stream
+        // products are left out of it (they overlap the restart kernel).
+        Timer untimed;
+        Scoped sc(st ? untimed : timer, kTSpmvMul);
         Epilogue<T> e;
         const bool col_scale = ch.scale && ch.scale_column;
         if (ch.center) {
@@ -398,11 +419,11 @@ struct Engine {
                 e.iscale = svec;
                 e.idivide = ch.scale_divide;
             } else {
-                launch_scale_vector<T>(x, svec, ch.scale_divide, n, xtmp.as<T>(), stream);
+                launch_scale_vector<T>(x, svec, ch.scale_divide, n, xtmp.as<T>(), ms);
                 xin = xtmp.as<T>();
             }
         }
-        launch_spmv<T>(A.mul.dev, xin, y, partial.as<T>(), e, &ctrl->abort, stream);
+        launch_spmv<T>(A.mul.dev, xin, y, partial.as<T>(), e, &ctrl->abort, ms);
     }
 
     // adjoint: y (n) = Op^T x (m).  beta_adj must already hold the centring scalar.
@@ -438,10 +459,10 @@ struct Engine {
     const T* beta_mul_fscale() const { return (ch.scale && ch.scale_column && !ch.center_outer) ? svec : nullptr; }
     const T* beta_adj_fscale() const { return (ch.scale && !ch.scale_column && !ch.center_outer) ? svec : nullptr; }
 
-    void beta_mul_of(const T* x) {
+    void beta_mul_of(const T* x, cudaStream_t st = nullptr) {
         if (!ch.center) return;
         launch_beta<T>(x, n, beta_mul_fscale(), ch.scale_divide, cvec, &ctrl->beta_mul, part.as<double>(), ctrl,
-                       stream);
+                       st ? st : stream);
     }
     void beta_adj_of(const T* x) {
         if (!ch.center) return;
@@ -509,9 +530,17 @@ struct Engine {
     // synchronizes after each norm and refills from the host engine.
     void lanczos(int start, bool careful, std::mt19937_64& eng, int64_t& matvecs) {
         // W_next = A * V[:, start]
-        beta_mul_of(Vcol(start));
-        multiply(Vcol(start), Wn.as<T>(), nullptr, nullptr);
-        ++matvecs;
+        if (pre_ready && !careful) {
+            // Wn = (A'F) / ||F|| from the side stream; V[:, start] = F / ||F||.
+            CUDA_TRY(cudaStreamWaitEvent(stream, ev_pre, 0));
+            launch_normalize<T>(Wn.as<T>(), m, &ctrl->norm_F, nullptr, nullptr, 0, nullptr, nullptr,
+                                part.as<double>(), nullptr, -1, 0, ctrl, stream);
+        } else {
+            beta_mul_of(Vcol(start));
+            multiply(Vcol(start), Wn.as<T>(), nullptr, nullptr);
+            ++matvecs;
+        }
+        pre_ready = false;
         cgs(W.as<T>(), m, ldw, start, Wn.as<T>(), &ctrl->S, 0, 1);
         normalize_W(start, &ctrl->S);
         for (int j = start; j < work; ++j) {
@@ -631,6 +660,13 @@ struct Engine {
         int64_t matvecs = 0, steps = 0, careful_restarts = 0, svd_sweeps = 0;
         const DeviceInfo& di = device_info();
         const size_t restart_smem = di.max_smem_optin - 16384;
+        // FP32 form only: the FP64 form keeps the reference's order of operations.
+        const bool overlap = std::is_same<T, float>::value;
+        if (overlap && !side) {
+            CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+            CUDA_TRY(cudaEventCreateWithFlags(&ev_f, cudaEventDisableTiming));
+            CUDA_TRY(cudaEventCreateWithFlags(&ev_pre, cudaEventDisableTiming));
+        }
 
         auto reset_flags = [&]() {
             // abort, invariant, null_start back to zero (contiguous int32 fields).
@@ -655,12 +691,28 @@ struct Engine {
             ra.tol = tol;
             ra.svtol = svtol;
             ra.ctrl = ctrl;
+            if (overlap) CUDA_TRY(cudaEventRecord(ev_f, stream));
             {
                 Scoped sc(timer, kTRestart);
                 launch_restart(ra, stream, restart_smem);
             }
+            if (overlap) {
+                // Behind the restart kernel: Wn = A'F on the side stream.
+                CUDA_TRY(cudaStreamWaitEvent(side, ev_f, 0));
+                beta_mul_of(F.as<T>(), side);
+                multiply(F.as<T>(), Wn.as<T>(), nullptr, nullptr, side);
+                CUDA_TRY(cudaEventRecord(ev_pre, side));
+                ++matvecs;
+                pre_ready = true;
+            }
             Ctrl h;
             sync_ctrl(h);
+            if (overlap && (h.invariant || h.converged)) {
+                // The side product is not used: order it before what follows.
+                CUDA_TRY(cudaStreamWaitEvent(stream, ev_pre, 0));
+                if (pre_ready) --matvecs;
+                pre_ready = false;
+            }
             if (h.null_start) throw Error(IRLBA_GB300_ERROR_NUMERICAL, "starting vector near the null space of the input matrix");
             if (h.invariant) {
                 ++careful_restarts;

@@ -268,10 +268,105 @@ __global__ void __launch_bounds__(128) rotate_f32_tiled_kernel(const float* Q, i
     }
 }
 
+// FP32 rotation as a tiled GEMM for w, k <= 64. A CTA takes 128 rows at a
+// time and stages Q[rows, :w] in shared memory first, so the outputs may
+// overwrite Q (in place) and the fcol column may be one of the inputs. Each
+// of the 256 threads forms rows {4 tx .. 4 tx + 3, 64 + 4 tx .. 64 + 4 tx + 3}
+// x columns {4 ty .. 4 ty + 3}: per input column, three 16-byte shared loads
+// (conflict-free for the rows, broadcast for R) feed 32 FMAs.
+constexpr int kRotTileRows = 128;
+constexpr size_t kRotGemmSmem = sizeof(float) * (64 * 64 + 64 * kRotTileRows);
+
+__device__ __forceinline__ float4 load4_guarded(const float* src, int64_t r, int64_t L) {
+    if (r + 3 < L) return *reinterpret_cast<const float4*>(src);
+    float4 v;
+    v.x = r < L ? src[0] : 0.0f;
+    v.y = r + 1 < L ? src[1] : 0.0f;
+    v.z = r + 2 < L ? src[2] : 0.0f;
+    v.w = r + 3 < L ? src[3] : 0.0f;
+    return v;
+}
+
+__device__ __forceinline__ void store4_guarded(float* dst, int64_t r, int64_t L, float a, float b, float c, float d) {
+    if (r + 3 < L) {
+        *reinterpret_cast<float4*>(dst) = make_float4(a, b, c, d);
+        return;
+    }
+    if (r < L) dst[0] = a;
+    if (r + 1 < L) dst[1] = b;
+    if (r + 2 < L) dst[2] = c;
+}
+
+__global__ void __launch_bounds__(256) rotate_f32_gemm_kernel(const float* Q, int64_t L, int64_t ldq, int32_t w,
+                                                             const double* __restrict__ R, int32_t ldr, int32_t k,
+                                                             float* out, int64_t ldo, const float* __restrict__ fcol,
+                                                             const double* fnorm, const int32_t* abort) {
+    extern __shared__ __align__(16) float rsm[];
+    float* Rs = rsm;                // Rs[j * 64 + i]
+    float* Qs = rsm + 64 * 64;      // Qs[j * kRotTileRows + row]
+    if (abort && *abort) return;
+    for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
+        const int j = idx / 64, i = idx % 64;
+        Rs[idx] = (j < w && i < k) ? static_cast<float>(R[j + static_cast<int64_t>(i) * ldr]) : 0.0f;
+    }
+    const float finv = fcol ? static_cast<float>(1.0 / *fnorm) : 0.0f;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    for (int64_t r0 = blockIdx.x * static_cast<int64_t>(kRotTileRows); r0 < L;
+         r0 += static_cast<int64_t>(gridDim.x) * kRotTileRows) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < w * (kRotTileRows / 4); idx += blockDim.x) {
+            const int j = idx / (kRotTileRows / 4), q = idx % (kRotTileRows / 4);
+            const int64_t r = r0 + 4 * q;
+            *reinterpret_cast<float4*>(Qs + j * kRotTileRows + 4 * q) = load4_guarded(Q + r + j * ldq, r, L);
+        }
+        __syncthreads();
+        float acc[8][4];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
+        for (int j = 0; j < w; ++j) {
+            const float4 q0 = *reinterpret_cast<const float4*>(Qs + j * kRotTileRows + 4 * tx);
+            const float4 q1 = *reinterpret_cast<const float4*>(Qs + j * kRotTileRows + 64 + 4 * tx);
+            const float4 rr = *reinterpret_cast<const float4*>(Rs + j * 64 + 4 * ty);
+            const float qa[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+            const float rb[4] = {rr.x, rr.y, rr.z, rr.w};
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(qa[a], rb[b], acc[a][b]);
+        }
+        if (fcol)
+            for (int idx = threadIdx.x; idx < kRotTileRows; idx += blockDim.x) {
+                const int64_t r = r0 + idx;
+                if (r < L) out[r + static_cast<int64_t>(k) * ldo] = fcol[r] * finv;
+            }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int col = 4 * ty + b;
+            if (col < k) {
+                const int64_t ra = r0 + 4 * tx, rb2 = r0 + 64 + 4 * tx;
+                store4_guarded(out + ra + col * ldo, ra, L, acc[0][b], acc[1][b], acc[2][b], acc[3][b]);
+                store4_guarded(out + rb2 + col * ldo, rb2, L, acc[4][b], acc[5][b], acc[6][b], acc[7][b]);
+            }
+        }
+    }
+}
+
 template <typename T, typename O>
 void rotate_dispatch(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, O* out,
                      int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream) {
     if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value) {
+        const bool aligned = ldq % 4 == 0 && ldo % 4 == 0 && reinterpret_cast<uintptr_t>(Q) % 16 == 0 &&
+                             reinterpret_cast<uintptr_t>(out) % 16 == 0;
+        if (w <= 64 && k <= 64 && aligned) {
+            const int64_t tiles = (L + kRotTileRows - 1) / kRotTileRows;
+            const int grid = static_cast<int>(tiles < 152 * 4 ? (tiles < 1 ? 1 : tiles) : 152 * 4);
+            rotate_f32_gemm_kernel<<<grid, 256, kRotGemmSmem, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol,
+                                                                        fnorm, abort);
+            count_launch();
+            return;
+        }
         if (w <= 64) {
             const int grid = grid_for(L, 128, 152 * 16);
             if (w <= 16) {
