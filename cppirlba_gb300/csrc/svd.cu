@@ -103,155 +103,154 @@ __global__ void __launch_bounds__(kSvdThreads) restart_kernel(RestartArgs a, int
 }
 
 // ---------------------------------------------------------------------------
-// Restart step on a thread-block cluster. GB300 retires about two FP64 lane
-// operations per clock per SM, so one SM runs a 57 x 57 Jacobi sweep in about
-// half a millisecond. The cluster keeps G and V in CTA 0's shared memory and
-// gives each of its warps one column pair per round through distributed shared
-// memory; rounds are separated by cluster barriers. Within a CTA the rotation
-// parameters of its warps' pairs are derived by one thread each, in parallel
-// lanes. The arithmetic is the same as the single-CTA form (same ordering,
-// same formulas).
+// Restart step on a thread-block cluster, G and V distributed by rows. One-sided
+// Jacobi rotates column pairs; each CTA keeps a contiguous slice of the rows of
+// G and V in its own shared memory, forms the partial dot products of its rows
+// for every pair of the round, and publishes them; after one cluster barrier
+// every CTA adds the eight partials in rank order (so all CTAs hold identical
+// sums), derives the same rotations and applies them to its own rows. Column
+// norms follow Rutishauser's updates, identical in every CTA, and are
+// recomputed from partials once per sweep. Per round this is one cluster
+// barrier, eight distributed-shared-memory loads per pair and no remote
+// stores; the work per CTA is a few rows. At the end the slices are gathered
+// into CTA 0, which finishes the SVD and the restart tail.
+// Rotation: t = sign(zeta) |2g| / (|b - a| + sqrt((b - a)^2 + 4 g^2)) with
+// zeta = (b - a) / (2g) (Rutishauser's t without the zeta division),
+// c = 1 / sqrt(1 + t^2), s = c t.
 // ---------------------------------------------------------------------------
 constexpr int kClusterCTAs = 8;
 constexpr int kClusterThreads = 128;
-constexpr int kClusterMaxRows = 128;  // per-lane register cache: 4 rows
+constexpr int kClusterMaxN = 128;                               // work <= 128
+constexpr int kClusterRows = kClusterMaxN / kClusterCTAs;       // local rows per CTA
 
 __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kClusterThreads)
     restart_cluster_kernel(RestartArgs a) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
-    extern __shared__ __align__(16) double sm[];
-    __shared__ double norms_local[kClusterMaxRows];
-    __shared__ int order[kClusterMaxRows];
-    __shared__ int rotated_local;
-    __shared__ double pair_g[kClusterThreads / 32], pair_c[kClusterThreads / 32], pair_s[kClusterThreads / 32];
-    __shared__ int pair_p[kClusterThreads / 32], pair_q[kClusterThreads / 32];
-    const unsigned rank = cl.block_rank();
-    const int n = a.work;
-    const int nn = n * n;
+    extern __shared__ __align__(16) double sm[];   // CTA 0: gathered G and V (2 n^2 doubles)
+    __shared__ double Gl[kClusterRows][kClusterMaxN];
+    __shared__ double Vl[kClusterRows][kClusterMaxN];
+    __shared__ double part[2][kClusterMaxN];
+    __shared__ double nrm[kClusterMaxN];
+    __shared__ double pc[kClusterMaxN / 2], ps[kClusterMaxN / 2];
+    __shared__ double norms_local[kClusterMaxN];
+    __shared__ int order[kClusterMaxN];
+    __shared__ int rotated;
     // The abort flag does not change while the kernel runs: every CTA takes the
     // same branch, so no CTA waits at a barrier the others skip.
     if (a.ctrl->abort) return;
-    double* G = cl.map_shared_rank(sm, 0);
-    double* V = G + nn;
-    double* nrm = cl.map_shared_rank(norms_local, 0);
-    int* rotated = cl.map_shared_rank(&rotated_local, 0);
-    if (rank == 0) {
-        for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-            sm[e] = a.B[e];
-            sm[nn + e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
-        }
+    const int rank = static_cast<int>(cl.block_rank());
+    const int n = a.work;
+    const int r0 = n * rank / kClusterCTAs, r1 = n * (rank + 1) / kClusterCTAs, nr = r1 - r0;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < nr * n; e += blockDim.x) {
+        const int i = e / n, j = e % n;
+        Gl[i][j] = a.B[(r0 + i) + static_cast<int64_t>(j) * n];
+        Vl[i][j] = (r0 + i == j) ? 1.0 : 0.0;
     }
-    cl.sync();
+    __syncthreads();
 
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int gw = static_cast<int>(rank) * nw + warp;
-    const int gnw = static_cast<int>(cl.num_blocks()) * nw;
-    const int n2 = n + (n & 1);
+    const int n2 = n + (n & 1), half = n2 / 2;
     const double thresh = 2.220446049250313e-16 * static_cast<double>(n);
+    int buf = 0;
     int sweep = 0;
     for (; sweep < kMaxSweeps; ++sweep) {
-        for (int j = gw; j < n; j += gnw) {
+        for (int j = tid; j < n; j += blockDim.x) {
             double s = 0;
-            for (int i = lane; i < n; i += 32) {
-                const double x = G[j * n + i];
-                s += x * x;
-            }
-            s = warp_sum(s);
-            if (lane == 0) nrm[j] = s;
+            for (int i = 0; i < nr; ++i) s += Gl[i][j] * Gl[i][j];
+            part[buf][j] = s;
         }
-        if (rank == 0 && threadIdx.x == 0) *rotated = 0;
         cl.sync();
+        for (int j = tid; j < n; j += blockDim.x) {
+            double s = 0;
+            for (int r = 0; r < kClusterCTAs; ++r) s += cl.map_shared_rank(part[buf], r)[j];
+            nrm[j] = s;
+        }
+        buf ^= 1;
+        if (tid == 0) rotated = 0;
+        __syncthreads();
         for (int round = 0; round < n2 - 1; ++round) {
-            // Slots are taken gnw at a time so every thread runs the same
-            // number of phases. Phase 1: each warp caches its two columns and
-            // forms g; phase 2: one thread per local warp derives the rotation
-            // (the FP64 divides and square roots run in parallel lanes of one
-            // warp, not once per warp); phase 3: the warps rotate.
-            for (int base = 0; base < n2 / 2; base += gnw) {
-                const int slot = base + gw;
-                int p = 0, q = n;
-                if (slot < n2 / 2) {
-                    p = circle_partner_a(round, slot, n2);
-                    q = circle_partner_b(round, slot, n2);
-                    if (p > q) {
-                        const int tmp = p;
-                        p = q;
-                        q = tmp;
-                    }
+            for (int slot = tid; slot < half; slot += blockDim.x) {
+                int p = circle_partner_a(round, slot, n2);
+                int q = circle_partner_b(round, slot, n2);
+                if (p > q) {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
                 }
-                const bool live = q < n;
-                double* gp = G + p * n;
-                double* gq = G + q * n;
-                double xp[kClusterMaxRows / 32], xq[kClusterMaxRows / 32];
-                if (live) {
-                    double g = 0;
-#pragma unroll
-                    for (int u = 0; u < kClusterMaxRows / 32; ++u) {
-                        const int i = lane + 32 * u;
-                        xp[u] = i < n ? gp[i] : 0.0;
-                        xq[u] = i < n ? gq[i] : 0.0;
-                        g += xp[u] * xq[u];
-                    }
-                    g = warp_sum(g);
-                    if (lane == 0) {
-                        pair_g[warp] = g;
-                        pair_p[warp] = p;
-                        pair_q[warp] = q;
-                    }
-                } else if (lane == 0) {
-                    pair_q[warp] = n;
-                }
-                __syncthreads();
-                if (threadIdx.x < nw) {
-                    const int t = threadIdx.x;
-                    double c = 0, sn = 0;
-                    if (pair_q[t] < n) {
-                        const int pp = pair_p[t], qq = pair_q[t];
-                        const double g = pair_g[t];
-                        const double av = nrm[pp], bv = nrm[qq];
-                        if (!(g == 0.0 || fabs(g) <= thresh * sqrt(av * bv))) {
-                            const double zeta = (bv - av) / (2.0 * g);
-                            const double tt = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                            c = 1.0 / sqrt(1.0 + tt * tt);
-                            sn = c * tt;
-                            nrm[pp] = av - tt * g;
-                            nrm[qq] = bv + tt * g;
-                            *rotated = 1;
-                        }
-                    }
-                    pair_c[t] = c;
-                    pair_s[t] = sn;
-                }
-                __syncthreads();
-                const double c = pair_c[warp], sn = pair_s[warp];
-                if (live && c != 0.0) {
-                    double* vp = V + p * n;
-                    double* vq = V + q * n;
-#pragma unroll
-                    for (int u = 0; u < kClusterMaxRows / 32; ++u) {
-                        const int i = lane + 32 * u;
-                        if (i < n) {
-                            gp[i] = c * xp[u] - sn * xq[u];
-                            gq[i] = sn * xp[u] + c * xq[u];
-                            const double y = vp[i], z = vq[i];
-                            vp[i] = c * y - sn * z;
-                            vq[i] = sn * y + c * z;
-                        }
-                    }
-                }
-                __syncthreads();
+                double g = 0;
+                if (q < n)
+                    for (int i = 0; i < nr; ++i) g += Gl[i][p] * Gl[i][q];
+                part[buf][slot] = g;
             }
             cl.sync();
+            for (int slot = tid; slot < half; slot += blockDim.x) {
+                int p = circle_partner_a(round, slot, n2);
+                int q = circle_partner_b(round, slot, n2);
+                if (p > q) {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                double c = 0, sn = 0;
+                if (q < n) {
+                    double g = 0;
+                    for (int r = 0; r < kClusterCTAs; ++r) g += cl.map_shared_rank(part[buf], r)[slot];
+                    const double av = nrm[p], bv = nrm[q];
+                    if (!(g == 0.0 || fabs(g) <= thresh * sqrt(av * bv))) {
+                        const double d = bv - av;
+                        const double t = (d >= 0 ? 1.0 : -1.0) * (g >= 0 ? 1.0 : -1.0) * fabs(2.0 * g) /
+                                         (fabs(d) + sqrt(d * d + 4.0 * g * g));
+                        c = rsqrt(1.0 + t * t);
+                        sn = c * t;
+                        nrm[p] = av - t * g;
+                        nrm[q] = bv + t * g;
+                        rotated = 1;
+                    }
+                }
+                pc[slot] = c;
+                ps[slot] = sn;
+            }
+            buf ^= 1;
+            __syncthreads();
+            for (int e = tid; e < half * nr; e += blockDim.x) {
+                const int slot = e / nr, i = e % nr;
+                const double c = pc[slot];
+                if (c == 0.0) continue;
+                const double sn = ps[slot];
+                int p = circle_partner_a(round, slot, n2);
+                int q = circle_partner_b(round, slot, n2);
+                if (p > q) {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                const double x = Gl[i][p], y = Gl[i][q];
+                Gl[i][p] = c * x - sn * y;
+                Gl[i][q] = sn * x + c * y;
+                const double u = Vl[i][p], v = Vl[i][q];
+                Vl[i][p] = c * u - sn * v;
+                Vl[i][q] = sn * u + c * v;
+            }
+            __syncthreads();
         }
-        const int any = *rotated;
-        cl.sync();
+        // Every CTA made the same decisions, so `rotated` agrees across the cluster.
+        const int any = rotated;
+        __syncthreads();
         if (!any) break;
     }
-    // CTA 0 finishes; the others stop touching its shared memory after the
-    // last barrier above and may exit.
+    // Gather the row slices into CTA 0 (column-major G, then V), then CTA 0
+    // finishes; the others are done with distributed shared memory after the
+    // barrier and may exit.
+    double* G0 = cl.map_shared_rank(sm, 0);
+    for (int e = tid; e < nr * n; e += blockDim.x) {
+        const int i = e / n, j = e % n;
+        G0[(r0 + i) + j * n] = Gl[i][j];
+        G0[n * n + (r0 + i) + j * n] = Vl[i][j];
+    }
+    cl.sync();
     if (rank != 0) return;
-    finish_svd(sm, n, n, sm + nn, a.BS, a.BU, n, a.BV, n, norms_local, order);
+    finish_svd(sm, n, n, sm + n * n, a.BS, a.BU, n, a.BV, n, norms_local, order);
     restart_tail(a, sweep + 1, sweep >= kMaxSweeps ? 1 : 0);
 }
 
@@ -304,7 +303,7 @@ cudaError_t restart_configure(size_t smem_optin) {
 
 void launch_restart(const RestartArgs& a, cudaStream_t stream, size_t /*max_smem*/) {
     const size_t need = restart_smem_bytes(a.work);
-    if (a.work <= kClusterMaxRows && need <= g_restart_cluster_max_dynamic) {
+    if (a.work <= kClusterMaxN && need <= g_restart_cluster_max_dynamic) {
         restart_cluster_kernel<<<kClusterCTAs, kClusterThreads, need, stream>>>(a);
         count_launch();
         return;
