@@ -147,6 +147,7 @@ def load_library():
         "irlba_gb300_matrix_layout": (i32, [P, ctypes.POINTER(i64), ctypes.POINTER(i32), ctypes.POINTER(i32),
                                             ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]),
         "irlba_gb300_set_profiling": (None, [i32]),
+        "irlba_gb300_set_device_ingest": (None, [i32]),
         "irlba_gb300_last_profile": (None, [pd, ctypes.POINTER(i64)]),
         "irlba_gb300_launch_count": (i64, []),
         "irlba_gb300_transfer_bytes": (None, [ctypes.POINTER(i64), ctypes.POINTER(i64)]),
@@ -443,6 +444,11 @@ def pca(matrix, center, scale, number, options=None):
 
 def device_count():
     return load_library().irlba_gb300_device_count()
+
+
+def set_device_ingest(on):
+    """Build sparse matrices' device layout on the GPU (default) or on the host."""
+    load_library().irlba_gb300_set_device_ingest(int(bool(on)))
 
 
 def set_profiling(on):

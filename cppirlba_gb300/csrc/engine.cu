@@ -269,6 +269,115 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
 }
 
 // ---------------------------------------------------------------------------
+// Device-side ingestion: the same plans built on the GPU from the uploaded
+// compressed arrays (ingest.cu). Rows must be sorted; pointers are checked on
+// the host first, so every device read stays inside the uploaded arrays.
+// ---------------------------------------------------------------------------
+static bool g_device_ingest = true;
+
+struct DevCompressed {
+    int64_t rows = 0, cols = 0, nnz = 0;
+    const int64_t* ptr = nullptr;
+    const int32_t* idx = nullptr;
+    const void* val = nullptr;
+    bool f64 = false;
+};
+
+static void build_plan_device(const DevCompressed& h, bool store_f64, bool x_f64, DirPlan& plan, cudaStream_t s) {
+    const DeviceInfo& di = device_info();
+    DirPlanDev& d = plan.dev;
+    d.nrows = h.rows;
+    d.ncols = h.cols;
+    d.nnz = h.nnz;
+    d.val_f64 = store_f64 ? 1 : 0;
+    const size_t xbytes = x_f64 ? 8 : 4;
+    const int64_t pw_max = static_cast<int64_t>(kPanelBytes / xbytes);
+    int64_t npanels = 1;
+    bool staged = true;
+    const int64_t pw = std::max<int64_t>(1, std::min<int64_t>(h.cols, pw_max));
+    if (h.cols > pw_max) {
+        npanels = (h.cols + pw_max - 1) / pw_max;
+        const double avg = static_cast<double>(d.nnz) / (static_cast<double>(h.rows) * static_cast<double>(npanels));
+        if (avg < 4.0 || npanels > (1 << 20)) {
+            staged = false;
+            npanels = 1;
+        }
+    }
+    d.staged = staged ? 1 : 0;
+    d.npanels = static_cast<int32_t>(npanels);
+    d.panel_width = staged ? pw : h.cols;
+    d.nseg = npanels * h.rows;
+    const int64_t R = h.rows, nnz = d.nnz, nseg = d.nseg;
+    plan.segptr.alloc(sizeof(int64_t) * (nseg + 1));
+    plan.idx.alloc(std::max<size_t>((staged ? sizeof(uint16_t) : sizeof(int32_t)) * nnz, 16));
+    plan.val.alloc(std::max<size_t>((store_f64 ? sizeof(double) : sizeof(float)) * nnz, 16));
+    uint16_t* idx16 = staged ? plan.idx.as<uint16_t>() : nullptr;
+    int32_t* idx32 = staged ? nullptr : plan.idx.as<int32_t>();
+    if (!staged || npanels == 1) {
+        CUDA_TRY(cudaMemcpyAsync(plan.segptr.ptr, h.ptr, sizeof(int64_t) * (R + 1), cudaMemcpyDeviceToDevice, s));
+        launch_copy_entries(nnz, h.idx, h.val, h.f64, idx16, idx32, plan.val.ptr, store_f64, s);
+    } else {
+        DevBuf cnt(sizeof(int64_t) * std::max<int64_t>(nseg, 1)), scr(sizeof(int64_t) * scan_scratch_elems(nseg));
+        launch_panel_count(R, static_cast<int32_t>(npanels), pw, h.ptr, h.idx, cnt.as<int64_t>(), s);
+        launch_exclusive_scan(cnt.as<int64_t>(), nseg, plan.segptr.as<int64_t>(), plan.segptr.as<int64_t>() + nseg,
+                              scr.as<int64_t>(), s);
+        launch_panel_scatter(R, static_cast<int32_t>(npanels), pw, h.ptr, h.idx, h.val, h.f64,
+                             plan.segptr.as<int64_t>(), idx16, plan.val.ptr, store_f64, s);
+        CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    d.smem_bytes = staged ? static_cast<size_t>(d.panel_width) * xbytes : 0;
+    {
+        const double avg = nseg > 0 ? static_cast<double>(nnz) / static_cast<double>(nseg) : 0.0;
+        const double vecs = avg / (store_f64 ? 2.0 : 4.0);
+        d.group_lanes = vecs >= 96 ? 32 : vecs >= 24 ? 16 : vecs >= 6 ? 8 : 4;
+    }
+    const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes, d.group_lanes);
+    int64_t nblocks = static_cast<int64_t>(di.sms) * per_sm;
+    const int64_t total_cost = nnz + kSegCost * nseg;
+    nblocks = std::max<int64_t>(1, std::min<int64_t>(nblocks, std::max<int64_t>(1, total_cost / 2048)));
+    plan.block_seg.alloc(sizeof(int64_t) * (nblocks + 1));
+    launch_block_seg(plan.segptr.as<int64_t>(), nseg, kSegCost, nblocks, plan.block_seg.as<int64_t>(), s);
+    d.nblocks = static_cast<int32_t>(nblocks);
+    d.segptr = plan.segptr.as<int64_t>();
+    d.idx16 = idx16;
+    d.idx32 = idx32;
+    d.val = plan.val.ptr;
+    d.block_seg = plan.block_seg.as<int64_t>();
+}
+
+// Stable transpose of a device compressed matrix (entries of each output row
+// in increasing input-row order); hptr: the input pointers on the host, for
+// nnz-balanced chunks of input rows.
+static void transpose_device(const DevCompressed& in, const int64_t* hptr, bool out_f64, DevBuf& tptr, DevBuf& tidx,
+                             DevBuf& tval, cudaStream_t s) {
+    const int64_t R = in.rows, C = in.cols, nnz = in.nnz;
+    const int64_t budget = 512ll << 20;  // bytes of chunk counters (int32 counts + int64 cursors)
+    int nchunks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({256, std::max<int64_t>(R, 1),
+                                                                          budget / (12 * std::max<int64_t>(C, 1))})));
+    std::vector<int64_t> chunk_rows(nchunks + 1, 0);
+    for (int c = 1; c < nchunks; ++c) {
+        const int64_t target = nnz * c / nchunks;
+        chunk_rows[c] = std::lower_bound(hptr, hptr + R + 1, target) - hptr;
+        chunk_rows[c] = std::max(chunk_rows[c], chunk_rows[c - 1]);
+    }
+    chunk_rows[nchunks] = R;
+    DevBuf dchunks = upload(chunk_rows.data(), chunk_rows.size());
+    tptr.alloc(sizeof(int64_t) * (C + 1));
+    tidx.alloc(std::max<size_t>(sizeof(int32_t) * nnz, 16));
+    tval.alloc(std::max<size_t>((out_f64 ? sizeof(double) : sizeof(float)) * nnz, 16));
+    DevBuf count(sizeof(int32_t) * std::max<int64_t>(nchunks * C, 1)),
+        cursor(sizeof(int64_t) * std::max<int64_t>(nchunks * C, 1)), scr(sizeof(int64_t) * scan_scratch_elems(C));
+    CUDA_TRY(cudaMemsetAsync(count.ptr, 0, count.bytes, s));
+    launch_transpose_count(in.ptr, in.idx, dchunks.as<int64_t>(), nchunks, C, count.as<int32_t>(), s);
+    launch_transpose_totals(count.as<int32_t>(), nchunks, C, tptr.as<int64_t>(), s);
+    launch_exclusive_scan(tptr.as<int64_t>(), C, tptr.as<int64_t>(), tptr.as<int64_t>() + C, scr.as<int64_t>(), s);
+    launch_transpose_cursors(count.as<int32_t>(), nchunks, C, tptr.as<int64_t>(), cursor.as<int64_t>(), s);
+    launch_transpose_scatter(in.ptr, in.idx, in.val, in.f64, dchunks.as<int64_t>(), nchunks, C,
+                             cursor.as<int64_t>(), tidx.as<int32_t>(), tval.ptr, out_f64, s);
+    CUDA_TRY(cudaStreamSynchronize(s));
+}
+
+// ---------------------------------------------------------------------------
 // Matrix handles
 // ---------------------------------------------------------------------------
 // ---------------------------------------------------------------------------
@@ -1070,15 +1179,7 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
         if (pointers[0] != 0) invalid("pointers must start at zero");
         for (int64_t p = 0; p < primary; ++p)
             if (pointers[p + 1] < pointers[p]) invalid("pointers must be non-decreasing");
-        std::atomic<int> bad_index{0};
-        parallel_rows(pointers, primary, [&](int64_t b, int64_t e, int) {
-            for (int64_t s = pointers[b]; s < pointers[e]; ++s)
-                if (indices[s] < 0 || indices[s] >= secondary) {
-                    bad_index.store(1);
-                    break;
-                }
-        });
-        if (bad_index.load()) invalid("index out of range of the secondary dimension");
+        const int64_t nnz = pointers[primary];
         device_info();
         auto base = std::make_shared<BaseMatrix>();
         base->nrow = nrow;
@@ -1087,22 +1188,77 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
         const bool in_f64 = value_type == IRLBA_GB300_VALUE_F64;
         base->store_f64 = (form == IRLBA_GB300_FORM_FP64) && in_f64;
         const bool x_f64 = form == IRLBA_GB300_FORM_FP64;
-        HostCompressed native;
-        native.rows = primary;
-        native.cols = secondary;
-        native.ptr = pointers;
-        native.idx = indices;
-        native.val = values;
-        native.f64 = in_f64;
-        HostCompressed trans;
-        transpose_host(native, trans);
-        // native rows = primary. column_major: primary = columns -> adjoint gather.
-        if (column_major) {
-            build_plan(native, base->store_f64, x_f64, base->adj);
-            build_plan(trans, base->store_f64, x_f64, base->mul);
-        } else {
-            build_plan(native, base->store_f64, x_f64, base->mul);
-            build_plan(trans, base->store_f64, x_f64, base->adj);
+        bool done = false;
+        if (g_device_ingest && nnz > 0) {
+            // Upload the compressed arrays, check them and build both plans on the device.
+            StreamGuard sg;
+            const cudaStream_t s = sg.s;
+            DevBuf dptr(sizeof(int64_t) * (primary + 1)), didx(sizeof(int32_t) * nnz),
+                dval((in_f64 ? sizeof(double) : sizeof(float)) * nnz), flags(sizeof(int32_t) * 4);
+            CUDA_TRY(h2d_async(dptr.ptr, pointers, dptr.bytes, s));
+            CUDA_TRY(h2d_async(didx.ptr, indices, didx.bytes, s));
+            CUDA_TRY(h2d_async(dval.ptr, values, dval.bytes, s));
+            CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, flags.bytes, s));
+            launch_validate(primary, secondary, dptr.as<int64_t>(), didx.as<int32_t>(), flags.as<int32_t>(), s);
+            int32_t hf[4] = {0, 0, 0, 0};
+            CUDA_TRY(d2h_async(hf, flags.ptr, sizeof(hf), s));
+            CUDA_TRY(cudaStreamSynchronize(s));
+            if (hf[1]) invalid("index out of range of the secondary dimension");
+            if (!hf[2]) {
+                DevCompressed native;
+                native.rows = primary;
+                native.cols = secondary;
+                native.nnz = nnz;
+                native.ptr = dptr.as<int64_t>();
+                native.idx = didx.as<int32_t>();
+                native.val = dval.ptr;
+                native.f64 = in_f64;
+                DevBuf tptr, tidx, tval;
+                transpose_device(native, pointers, base->store_f64, tptr, tidx, tval, s);
+                DevCompressed trans;
+                trans.rows = secondary;
+                trans.cols = primary;
+                trans.nnz = nnz;
+                trans.ptr = tptr.as<int64_t>();
+                trans.idx = tidx.as<int32_t>();
+                trans.val = tval.ptr;
+                trans.f64 = base->store_f64;
+                // native rows = primary. column_major: primary = columns -> adjoint gather.
+                build_plan_device(native, base->store_f64, x_f64, column_major ? base->adj : base->mul, s);
+                build_plan_device(trans, base->store_f64, x_f64, column_major ? base->mul : base->adj, s);
+                CUDA_TRY(cudaStreamSynchronize(s));
+                CUDA_TRY(cudaGetLastError());
+                done = true;
+            }
+        }
+        if (!done) {
+            // Host ingestion (unsorted rows, or device ingestion switched off).
+            std::atomic<int> bad_index{0};
+            parallel_rows(pointers, primary, [&](int64_t b, int64_t e, int) {
+                for (int64_t s = pointers[b]; s < pointers[e]; ++s)
+                    if (indices[s] < 0 || indices[s] >= secondary) {
+                        bad_index.store(1);
+                        break;
+                    }
+            });
+            if (bad_index.load()) invalid("index out of range of the secondary dimension");
+            HostCompressed native;
+            native.rows = primary;
+            native.cols = secondary;
+            native.ptr = pointers;
+            native.idx = indices;
+            native.val = values;
+            native.f64 = in_f64;
+            HostCompressed trans;
+            transpose_host(native, trans);
+            // native rows = primary. column_major: primary = columns -> adjoint gather.
+            if (column_major) {
+                build_plan(native, base->store_f64, x_f64, base->adj);
+                build_plan(trans, base->store_f64, x_f64, base->mul);
+            } else {
+                build_plan(native, base->store_f64, x_f64, base->mul);
+                build_plan(trans, base->store_f64, x_f64, base->adj);
+            }
         }
         auto* h = new irlba_gb300_matrix();
         h->kind = 0;
@@ -1113,6 +1269,8 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
         *out = h;
     });
 }
+
+void irlba_gb300_set_device_ingest(int32_t on) { g_device_ingest = on != 0; }
 
 irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, const void* values,
                                                    irlba_gb300_value_type value_type, int64_t ld, int32_t row_major,

@@ -216,6 +216,36 @@ struct BatchResult {
 };
 
 // ---------------------------------------------------------------------------
+// Device-side ingestion (ingest.cu): compressed arrays -> gather plans.
+// ---------------------------------------------------------------------------
+// flags[0] pointer error, flags[1] index out of range, flags[2] unsorted row.
+void launch_validate(int64_t rows, int64_t cols, const int64_t* ptr, const int32_t* idx, int32_t* flags,
+                     cudaStream_t s);
+// Exclusive scan of n int64 (out may alias in); *total = sum; scratch >= scan_scratch_elems(n).
+size_t scan_scratch_elems(int64_t n);
+void launch_exclusive_scan(const int64_t* in, int64_t n, int64_t* out, int64_t* total, int64_t* scratch,
+                           cudaStream_t s);
+// Stable transpose over chunks of input rows (chunk_rows: nchunks + 1 boundaries).
+void launch_transpose_count(const int64_t* ptr, const int32_t* idx, const int64_t* chunk_rows, int nchunks,
+                            int64_t cols, int32_t* count, cudaStream_t s);
+void launch_transpose_totals(const int32_t* count, int nchunks, int64_t cols, int64_t* tot, cudaStream_t s);
+void launch_transpose_cursors(const int32_t* count, int nchunks, int64_t cols, const int64_t* tptr, int64_t* cursor,
+                              cudaStream_t s);
+void launch_transpose_scatter(const int64_t* ptr, const int32_t* idx, const void* val, bool in_f64,
+                              const int64_t* chunk_rows, int nchunks, int64_t cols, int64_t* cursor, int32_t* tidx,
+                              void* tval, bool out_f64, cudaStream_t s);
+// Panel layout of sorted rows: counts per (panel, row), then the panel-major copy.
+void launch_panel_count(int64_t rows, int32_t npanels, int64_t pw, const int64_t* ptr, const int32_t* idx,
+                        int64_t* cnt, cudaStream_t s);
+void launch_panel_scatter(int64_t rows, int32_t npanels, int64_t pw, const int64_t* ptr, const int32_t* idx,
+                          const void* val, bool in_f64, const int64_t* segptr, uint16_t* idx16, void* vout,
+                          bool out_f64, cudaStream_t s);
+void launch_copy_entries(int64_t nnz, const int32_t* idx, const void* val, bool in_f64, uint16_t* idx16,
+                         int32_t* idx32, void* vout, bool out_f64, cudaStream_t s);
+void launch_block_seg(const int64_t* segptr, int64_t nseg, int64_t cost, int64_t nblocks, int64_t* bseg,
+                      cudaStream_t s);
+
+// ---------------------------------------------------------------------------
 // Differentiation form (adjoint.cu). Blocks are row-major FP64 with k <= 64
 // columns; Z1 and Z2 have kk = 2k <= 128.
 // ---------------------------------------------------------------------------

@@ -99,6 +99,12 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
                                                     const int64_t* pointers, int32_t column_major,
                                                     irlba_gb300_form form, irlba_gb300_matrix** out);
 
+/* Where irlba_gb300_matrix_create_sparse builds its device layout: on the GPU
+ * from the uploaded compressed arrays (default; needs about twice the matrix
+ * size of device memory while it runs, and sorted rows, else it uses the
+ * host), or on the host (on = 0). Both give the same layout. */
+void irlba_gb300_set_device_ingest(int32_t on);
+
 /* SimpleMatrix over a dense matrix (simple.hpp:124-178); column-major unless
  * row_major != 0; `ld` is the leading dimension. Copied to the device. */
 irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, const void* values,
