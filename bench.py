@@ -73,6 +73,18 @@ def dist_setup():
     return world, rank, local
 
 
+def reduce_max(x, device):
+    """Largest value of x over the ranks of the default process group (x when
+    there is none or it has one rank); the timed value is the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -419,11 +431,7 @@ def main():
             torch.distributed.barrier()
 
     def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, "cuda")
 
     eng.load_library()
     t_gen = time.perf_counter()
