@@ -223,7 +223,8 @@ class Options:
 
 @dataclass
 class Results:
-    """irlba::Results (compute.hpp:357-388)."""
+    """irlba::Results (compute.hpp:357-388). U and V are column-major
+    (Fortran-ordered) like the reference's Eigen matrices."""
 
     U: np.ndarray
     V: np.ndarray
@@ -235,7 +236,8 @@ class Results:
 
 @dataclass
 class PcaResults:
-    """irlba::PcaResults (pca.hpp:146-179)."""
+    """irlba::PcaResults (pca.hpp:146-179). scores and rotation are
+    column-major (Fortran-ordered) like the reference's Eigen matrices."""
 
     scores: np.ndarray
     rotation: np.ndarray
@@ -389,8 +391,8 @@ def compute(matrix, number, options=None):
     o = options._to_c(keep)
     m, n = matrix.rows(), matrix.cols()
     cap = max(min(number, min(m, n)), 0)
-    U = np.zeros((cap, m))
-    V = np.zeros((cap, n))
+    U = np.empty((cap, m))  # column-major m x cap, as the C ABI writes it
+    V = np.empty((cap, n))
     D = np.zeros(max(cap, 1))
     num = ctypes.c_int64()
     conv = ctypes.c_int32()
@@ -400,7 +402,7 @@ def compute(matrix, number, options=None):
                                               ctypes.byref(num), ctypes.byref(conv), ctypes.byref(iters),
                                               ctypes.byref(st)))
     r = num.value
-    return Results(U=U[:r].T.copy(), V=V[:r].T.copy(), D=D[:r].copy(), iterations=iters.value,
+    return Results(U=U[:r].T, V=V[:r].T, D=D[:r].copy(), iterations=iters.value,
                    converged=bool(conv.value), stats=_stats_dict(st))
 
 
@@ -422,8 +424,8 @@ def pca(matrix, center, scale, number, options=None):
     o = options._to_c(keep)
     m, n = matrix.rows(), matrix.cols()
     cap = max(min(number, min(m, n)), 0)
-    S = np.zeros((cap, m))
-    R = np.zeros((cap, n))
+    S = np.empty((cap, m))  # column-major m x cap, as the C ABI writes it
+    R = np.empty((cap, n))
     var = np.zeros(max(cap, 1))
     c_out = np.zeros(max(n, 1))
     s_out = np.zeros(max(n, 1))
@@ -436,7 +438,7 @@ def pca(matrix, center, scale, number, options=None):
                                           ctypes.byref(conv), ctypes.byref(iters), _dptr(c_out), _dptr(s_out),
                                           ctypes.byref(st)))
     r = num.value
-    return PcaResults(scores=S[:r].T.copy(), rotation=R[:r].T.copy(), variances=var[:r].copy(),
+    return PcaResults(scores=S[:r].T, rotation=R[:r].T, variances=var[:r].copy(),
                       iterations=iters.value, converged=bool(conv.value),
                       center=c_out[:n].copy() if center else None, scale=s_out[:n].copy() if scale else None,
                       stats=_stats_dict(st))
@@ -557,8 +559,8 @@ class Batch:
             _check(load_library().irlba_gb300_batch_result(self._h, j, None, None, None, None, None, None))
         m, n = int(self.nrow[j]), int(self.ncol[j])
         r = max(min(self._number, min(m, n)), 0)
-        S = np.zeros((max(self._number, 1), m))
-        R = np.zeros((max(self._number, 1), n))
+        S = np.empty((max(self._number, 1), m))
+        R = np.empty((max(self._number, 1), n))
         var = np.zeros(max(self._number, 1))
         c_out = np.zeros(max(n, 1))
         s_out = np.zeros(max(n, 1))
@@ -566,7 +568,7 @@ class Batch:
         _check(load_library().irlba_gb300_batch_result(self._h, j, _dptr(S), _dptr(R), _dptr(var), _dptr(c_out),
                                                        _dptr(s_out), ctypes.byref(inf)))
         info = {f: getattr(inf, f) for f, _ in BatchInfo._fields_}
-        return PcaResults(scores=S[:r].T.copy(), rotation=R[:r].T.copy(), variances=var[:r].copy(),
+        return PcaResults(scores=S[:r].T, rotation=R[:r].T, variances=var[:r].copy(),
                           iterations=inf.iterations, converged=bool(inf.converged),
                           center=c_out[:n].copy() if self._center else None,
                           scale=s_out[:n].copy() if self._scale else None, stats=info)

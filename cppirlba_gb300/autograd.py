@@ -5,7 +5,9 @@ autograd operations, backed by libtorch C++ torch::autograd::Function classes
 truncated_svd(A, k)  -> (U, S, V) of a dense CUDA matrix (FP32 uses the
     FP32+FP64-steps form, FP64 the plain form); backward: the truncated-SVD
     adjoint (F-matrix terms, plus the orthogonal-complement terms solved by
-    shifted conjugate gradients, cg_tol < 0 for the rank-k projection terms).
+    shifted conjugate gradients to relative residual cg_tol: by default 1e-8
+    for FP32 input and 1e-12 for FP64; cg_tol < 0 for the rank-k projection
+    terms).
 sparse_pca_svd(values, pointers, indices, nrow, ncol, column_major, center,
     scale, k) -> (U, S, V, center, scale) of pca()'s centred/scaled operator of
     a compressed sparse matrix; backward: the gradient on the stored values
@@ -40,14 +42,22 @@ def load_extension():
     return _ext
 
 
-def truncated_svd(A, k, tol=1e-10, seed=5489, cg_tol=1e-12, cg_max_iter=5000):
-    return load_extension().truncated_svd(A, int(k), float(tol), int(seed), float(cg_tol), int(cg_max_iter))
+def _cg_tol(cg_tol, dtype):
+    # The complement solves need no more accuracy than the forward carries.
+    if cg_tol is not None:
+        return float(cg_tol)
+    return 1e-8 if dtype == torch.float32 else 1e-12
+
+
+def truncated_svd(A, k, tol=1e-10, seed=5489, cg_tol=None, cg_max_iter=5000):
+    return load_extension().truncated_svd(A, int(k), float(tol), int(seed), _cg_tol(cg_tol, A.dtype),
+                                          int(cg_max_iter))
 
 
 def sparse_pca_svd(values, pointers, indices, nrow, ncol, column_major, center, scale, k, tol=1e-10, seed=5489,
-                   cg_tol=1e-12, cg_max_iter=5000, statistics=True):
+                   cg_tol=None, cg_max_iter=5000, statistics=True):
     pointers = torch.as_tensor(pointers, dtype=torch.int64).contiguous().cpu()
     indices = torch.as_tensor(indices, dtype=torch.int32).contiguous().cpu()
     return load_extension().sparse_pca_svd(values, pointers, indices, int(nrow), int(ncol), bool(column_major),
-                                           bool(center), bool(scale), int(k), float(tol), int(seed), float(cg_tol),
-                                           int(cg_max_iter), bool(statistics))
+                                           bool(center), bool(scale), int(k), float(tol), int(seed),
+                                           _cg_tol(cg_tol, values.dtype), int(cg_max_iter), bool(statistics))

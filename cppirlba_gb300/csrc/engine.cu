@@ -351,8 +351,12 @@ static void build_plan_device(const DevCompressed& h, bool store_f64, bool x_f64
 static void transpose_device(const DevCompressed& in, const int64_t* hptr, bool out_f64, DevBuf& tptr, DevBuf& tidx,
                              DevBuf& tval, cudaStream_t s) {
     const int64_t R = in.rows, C = in.cols, nnz = in.nnz;
-    const int64_t budget = 512ll << 20;  // bytes of chunk counters (int32 counts + int64 cursors)
-    int nchunks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({256, std::max<int64_t>(R, 1),
+    // Bytes of chunk counters (int32 counts + int64 cursors): up to 2 GiB or an
+    // eighth of the free device memory; more chunks keep more SMs scattering.
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    const int64_t budget = std::min<int64_t>(2ll << 30, static_cast<int64_t>(free_b / 8));
+    int nchunks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({304, std::max<int64_t>(R, 1),
                                                                           budget / (12 * std::max<int64_t>(C, 1))})));
     std::vector<int64_t> chunk_rows(nchunks + 1, 0);
     for (int c = 1; c < nchunks; ++c) {
@@ -1199,7 +1203,7 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
             CUDA_TRY(h2d_async(didx.ptr, indices, didx.bytes, s));
             CUDA_TRY(h2d_async(dval.ptr, values, dval.bytes, s));
             CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, flags.bytes, s));
-            launch_validate(primary, secondary, dptr.as<int64_t>(), didx.as<int32_t>(), flags.as<int32_t>(), s);
+            launch_validate(primary, secondary, nnz, dptr.as<int64_t>(), didx.as<int32_t>(), flags.as<int32_t>(), s);
             int32_t hf[4] = {0, 0, 0, 0};
             CUDA_TRY(d2h_async(hf, flags.ptr, sizeof(hf), s));
             CUDA_TRY(cudaStreamSynchronize(s));

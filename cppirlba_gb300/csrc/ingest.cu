@@ -22,23 +22,24 @@ int grid_of(int64_t work, int cap) {
     return static_cast<int>(g);
 }
 
-// flags[0]: a pointer decreases or ends beyond nnz; flags[1]: an index is
-// outside [0, cols); flags[2]: a row is not sorted (non-decreasing).
-__global__ void validate_kernel(int64_t rows, int64_t cols, const int64_t* __restrict__ ptr,
+// flags[1]: an index is outside [0, cols); flags[2]: a row is not sorted
+// (non-decreasing). Element-parallel: entry s breaks the order when
+// idx[s] < idx[s - 1] and s does not start a row (checked by binary search on
+// the pointers, which the host has already checked).
+__global__ void validate_kernel(int64_t rows, int64_t cols, int64_t nnz, const int64_t* __restrict__ ptr,
                                 const int32_t* __restrict__ idx, int32_t* flags) {
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < rows;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t b = ptr[r], e = ptr[r + 1];
-        if (e < b) {
-            flags[0] = 1;
-            continue;
-        }
-        int32_t prev = -1;
-        for (int64_t s = b; s < e; ++s) {
-            const int32_t c = idx[s];
-            if (c < 0 || c >= cols) flags[1] = 1;
-            if (c < prev) flags[2] = 1;
-            prev = c;
+    for (int64_t s = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; s < nnz;
+         s += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int32_t c = idx[s];
+        if (c < 0 || c >= cols) flags[1] = 1;
+        if (s > 0 && c < idx[s - 1]) {
+            int64_t lo = 0, hi = rows;   // is there a row r with ptr[r] == s?
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (ptr[mid] < s) lo = mid + 1;
+                else hi = mid;
+            }
+            if (ptr[lo] != s) flags[2] = 1;
         }
     }
 }
@@ -278,10 +279,10 @@ void with_value_types(bool in_f64, bool out_f64, F f) {
 
 }  // namespace
 
-void launch_validate(int64_t rows, int64_t cols, const int64_t* ptr, const int32_t* idx, int32_t* flags,
-                     cudaStream_t s) {
-    if (rows == 0) return;
-    validate_kernel<<<grid_of(rows, 152 * 16), kT, 0, s>>>(rows, cols, ptr, idx, flags);
+void launch_validate(int64_t rows, int64_t cols, int64_t nnz, const int64_t* ptr, const int32_t* idx,
+                     int32_t* flags, cudaStream_t s) {
+    if (nnz == 0) return;
+    validate_kernel<<<grid_of(nnz, 152 * 16), kT, 0, s>>>(rows, cols, nnz, ptr, idx, flags);
     count_launch();
 }
 

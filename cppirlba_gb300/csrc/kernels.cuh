@@ -218,9 +218,9 @@ struct BatchResult {
 // ---------------------------------------------------------------------------
 // Device-side ingestion (ingest.cu): compressed arrays -> gather plans.
 // ---------------------------------------------------------------------------
-// flags[0] pointer error, flags[1] index out of range, flags[2] unsorted row.
-void launch_validate(int64_t rows, int64_t cols, const int64_t* ptr, const int32_t* idx, int32_t* flags,
-                     cudaStream_t s);
+// flags[1] index out of range, flags[2] unsorted row (pointers checked by the caller).
+void launch_validate(int64_t rows, int64_t cols, int64_t nnz, const int64_t* ptr, const int32_t* idx,
+                     int32_t* flags, cudaStream_t s);
 // Exclusive scan of n int64 (out may alias in); *total = sum; scratch >= scan_scratch_elems(n).
 size_t scan_scratch_elems(int64_t n);
 void launch_exclusive_scan(const int64_t* in, int64_t n, int64_t* out, int64_t* total, int64_t* scratch,
