@@ -148,6 +148,7 @@ def load_library():
                                             ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]),
         "irlba_gb300_set_profiling": (None, [i32]),
         "irlba_gb300_set_device_ingest": (None, [i32]),
+        "irlba_gb300_set_staging": (None, [i64, i64]),
         "irlba_gb300_last_profile": (None, [pd, ctypes.POINTER(i64)]),
         "irlba_gb300_launch_count": (i64, []),
         "irlba_gb300_transfer_bytes": (None, [ctypes.POINTER(i64), ctypes.POINTER(i64)]),
@@ -451,6 +452,12 @@ def device_count():
 def set_device_ingest(on):
     """Build sparse matrices' device layout on the GPU (default) or on the host."""
     load_library().irlba_gb300_set_device_ingest(int(bool(on)))
+
+
+def set_staging(min_bytes=16 << 20, slice_bytes=8 << 20):
+    """Copies of pageable host memory of at least `min_bytes` (< 0: never) go
+    through pinned staging buffers of `slice_bytes`, filled by host threads."""
+    load_library().irlba_gb300_set_staging(int(min_bytes), int(slice_bytes))
 
 
 def set_profiling(on):

@@ -63,21 +63,29 @@ inline irlba_gb300_status guarded(F f) {
 extern std::atomic<int64_t> g_h2d_bytes;
 extern std::atomic<int64_t> g_d2h_bytes;
 
+// Copies between host memory and the device (staging.cu): large copies of
+// pageable host memory go through pinned staging buffers filled by several
+// host threads; everything else is a plain cudaMemcpyAsync on `s`.
+cudaError_t copy_staged(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s);
+
 inline cudaError_t h2d_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     g_h2d_bytes.fetch_add(static_cast<int64_t>(bytes));
-    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+    return copy_staged(dst, src, bytes, cudaMemcpyHostToDevice, s);
 }
 inline cudaError_t d2h_async(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     g_d2h_bytes.fetch_add(static_cast<int64_t>(bytes));
-    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+    return copy_staged(dst, src, bytes, cudaMemcpyDeviceToHost, s);
 }
+// Synchronous forms, ordered on the default stream like cudaMemcpy.
 inline cudaError_t h2d_sync(void* dst, const void* src, size_t bytes) {
     g_h2d_bytes.fetch_add(static_cast<int64_t>(bytes));
-    return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    const cudaError_t e = copy_staged(dst, src, bytes, cudaMemcpyHostToDevice, 0);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(0);
 }
 inline cudaError_t d2h_sync(void* dst, const void* src, size_t bytes) {
     g_d2h_bytes.fetch_add(static_cast<int64_t>(bytes));
-    return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
+    const cudaError_t e = copy_staged(dst, src, bytes, cudaMemcpyDeviceToHost, 0);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(0);
 }
 
 // ---------------------------------------------------------------------------

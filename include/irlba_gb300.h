@@ -105,6 +105,13 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
  * host), or on the host (on = 0). Both give the same layout. */
 void irlba_gb300_set_device_ingest(int32_t on);
 
+/* Copies between pageable host memory and the device of at least `min_bytes`
+ * (default 16 MiB; < 0: never) run through pinned staging buffers of
+ * `slice_bytes` each (default 8 MiB; <= 0 keeps the current size), filled and
+ * drained by up to eight host threads. Smaller copies, and copies of pinned
+ * host memory, are plain cudaMemcpyAsync calls. Results are the same. */
+void irlba_gb300_set_staging(int64_t min_bytes, int64_t slice_bytes);
+
 /* SimpleMatrix over a dense matrix (simple.hpp:124-178); column-major unless
  * row_major != 0; `ld` is the leading dimension. Copied to the device. */
 irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, const void* values,

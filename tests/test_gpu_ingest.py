@@ -92,3 +92,42 @@ def test_unsorted_rows_and_index_errors(engine):
                 engine.ParallelSparseMatrix(200, 60, x, bad, p, True)
         finally:
             engine.set_device_ingest(True)
+
+
+@pytest.fixture
+def tiny_staging(engine):
+    """Stage every copy of 4 KiB or more through 4 KiB pinned slices (many
+    slices per worker, both buffers of every lane in use)."""
+    engine.set_staging(4096, 4096)
+    try:
+        yield
+    finally:
+        engine.set_staging(16 << 20, 8 << 20)
+
+
+@pytest.mark.parametrize("device_ingest", [True, False])
+def test_staged_copies_match_plain_copies(engine, tiny_staging, device_ingest):
+    from cppirlba_gb300 import datagen
+    inp = datagen.scrna_pca_input(300, 9000, 0.1, seed=31, dtype=np.float32, cell_major=False)
+    opts = engine.Options(seed=13)
+
+    def run():
+        engine.set_device_ingest(device_ingest)
+        try:
+            mat = engine.ParallelSparseMatrix(inp.nrow, inp.ncol, inp.val, inp.idx, inp.ptr, inp.column_major,
+                                              form=engine.FORM_FP32_FP64STEPS)
+        finally:
+            engine.set_device_ingest(True)
+        return mat, engine.pca(mat, True, True, 6, opts)
+
+    staged_mat, staged = run()
+    engine.set_staging(-1, 4096)
+    plain_mat, plain = run()
+    engine.set_staging(4096, 4096)
+    assert staged.scores.nbytes > 16 * 4096
+    np.testing.assert_array_equal(staged.scores, plain.scores)
+    np.testing.assert_array_equal(staged.rotation, plain.rotation)
+    np.testing.assert_array_equal(staged.variances, plain.variances)
+    # Most copies end in a partial slice (nnz * 4 bytes is no multiple of 4 KiB).
+    assert (inp.nnz * 4) % 4096 != 0
+    _same_products(engine, staged_mat, plain_mat, inp.nrow, inp.ncol)
