@@ -8,6 +8,7 @@ library is missing or no GPU is visible, the calls raise.
 """
 import ctypes
 import os
+import threading
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -127,6 +128,8 @@ def load_library():
         "irlba_gb300_device_count": (ctypes.c_int, []),
         "irlba_gb300_matrix_create_sparse": (i32, [i64, i64, P, i32, P, P, i32, i32, ctypes.POINTER(P)]),
         "irlba_gb300_matrix_create_dense": (i32, [i64, i64, P, i32, i64, i32, i32, ctypes.POINTER(P)]),
+        "irlba_gb300_matrix_create_device_operator": (i32, [i64, i64, P, P, i32, ctypes.POINTER(P)]),
+        "irlba_gb300_matrix_create_host_operator": (i32, [i64, i64, P, P, i32, ctypes.POINTER(P)]),
         "irlba_gb300_matrix_center": (i32, [P, pd, ctypes.POINTER(P)]),
         "irlba_gb300_matrix_scale": (i32, [P, pd, i32, i32, ctypes.POINTER(P)]),
         "irlba_gb300_matrix_destroy": (i32, [P]),
@@ -170,9 +173,18 @@ def load_library():
     return lib
 
 
+# The Python exception raised inside a user-defined product (OperatorMatrix,
+# DeviceOperatorMatrix) on this thread, re-raised as the cause of the failing call.
+_callback_state = threading.local()
+
+
 def _check(status):
     if status != OK:
         msg = load_library().irlba_gb300_last_error().decode()
+        cause = getattr(_callback_state, "error", None)
+        _callback_state.error = None
+        if cause is not None:
+            raise IrlbaError(status, msg) from cause
         raise IrlbaError(status, msg)
 
 
@@ -357,6 +369,75 @@ class SimpleMatrix(Matrix):
         _check(lib.irlba_gb300_matrix_create_dense(a.shape[0], a.shape[1], _vptr(buf), vt, max(ld, 1), row_major,
                                                    form, ctypes.byref(h)))
         super().__init__(h.value, a.shape[0], a.shape[1], form)
+
+
+# irlba_gb300_host_product / irlba_gb300_device_product (include/irlba_gb300.h).
+HOST_PRODUCT = ctypes.CFUNCTYPE(ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
+                                ctypes.POINTER(ctypes.c_double))
+DEVICE_PRODUCT = ctypes.CFUNCTYPE(ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p)
+
+
+class OperatorMatrix(Matrix):
+    """A user-defined irlba::Matrix (Matrix/interface.hpp:141-223) whose products
+    are Python callables on FP64 numpy vectors: multiply(x) returns A @ x (x of
+    length ncol) and adjoint_multiply(y) returns A.T @ y. The IRLBA loop stays on
+    the device; each product copies its vectors to the host and back (correct,
+    not fast). Centring and scaling decorators may wrap it; pca() may not."""
+
+    def __init__(self, nrow, ncol, multiply, adjoint_multiply, form=FORM_FP64):
+        lib = load_library()
+
+        def product(_user, adjoint, x, y):
+            try:
+                n_in, n_out = (nrow, ncol) if adjoint else (ncol, nrow)
+                xa = np.ctypeslib.as_array(x, shape=(n_in,)).copy()
+                res = np.asarray((adjoint_multiply if adjoint else multiply)(xa), dtype=np.float64)
+                if res.shape != (n_out,):
+                    raise ValueError("product returned shape %s, expected (%d,)" % (res.shape, n_out))
+                np.ctypeslib.as_array(y, shape=(n_out,))[:] = res
+                return 0
+            except BaseException as exc:  # reported through the engine's status
+                _callback_state.error = exc
+                return 1
+
+        cb = HOST_PRODUCT(product)
+        h = ctypes.c_void_p()
+        _check(lib.irlba_gb300_matrix_create_host_operator(nrow, ncol, ctypes.cast(cb, ctypes.c_void_p), None, form,
+                                                           ctypes.byref(h)))
+        super().__init__(h.value, nrow, ncol, form, keep=[cb])
+
+
+class DeviceOperatorMatrix(Matrix):
+    """A user-defined irlba::Matrix whose products run on the device, e.g. a
+    residual matrix that is never stored. `product(adjoint, x_ptr, y_ptr,
+    stream)` enqueues y = A x (adjoint False; x of length ncol) or y = A.T x on
+    the cudaStream_t `stream` (an int) and returns; x and y are device
+    addresses of float64 vectors (FORM_FP64) or float32 vectors
+    (FORM_FP32_FP64STEPS). `product` may instead be the address of a C function
+    with the irlba_gb300_device_product signature, with `user` its first
+    argument."""
+
+    def __init__(self, nrow, ncol, product, form=FORM_FP64, user=None):
+        lib = load_library()
+        keep = []
+        if callable(product):
+            def tramp(_user, adjoint, x, y, stream):
+                try:
+                    product(bool(adjoint), x or 0, y or 0, stream or 0)
+                    return 0
+                except BaseException as exc:  # reported through the engine's status
+                    _callback_state.error = exc
+                    return 1
+            cb = DEVICE_PRODUCT(tramp)
+            keep.append(cb)
+            fptr = ctypes.cast(cb, ctypes.c_void_p)
+        else:
+            fptr = ctypes.c_void_p(int(product))
+        h = ctypes.c_void_p()
+        _check(lib.irlba_gb300_matrix_create_device_operator(nrow, ncol, fptr, ctypes.c_void_p(user or 0), form,
+                                                             ctypes.byref(h)))
+        super().__init__(h.value, nrow, ncol, form, keep=keep)
 
 
 class CenteredMatrix(Matrix):

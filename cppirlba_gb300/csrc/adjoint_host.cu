@@ -194,6 +194,7 @@ irlba_gb300_status irlba_gb300_svd_adjoint_factors(const irlba_gb300_matrix* mat
         if (!matrix) invalid("matrix is NULL");
         if (!U || !S || !V || !Z1 || !Z2) invalid("U, S, V, Z1 and Z2 must not be NULL");
         const Chain ch = flatten(matrix);
+        require_stored(ch.base, "the differentiation form");
         const int64_t m = ch.base->nrow, n = ch.base->ncol;
         if (k < 1 || k > kAdjointMaxK) invalid("the SVD adjoint supports 1 <= k <= 64");
         if (k > std::min(m, n)) invalid("k cannot exceed the smaller matrix dimension");
@@ -311,6 +312,7 @@ irlba_gb300_status irlba_gb300_svd_adjoint_sparse(const irlba_gb300_matrix* matr
         if (!Z1 || !Z2 || !pointers || !indices || !values || !grad_values) invalid("array arguments must not be NULL");
         if (k < 1 || k > kAdjointMaxK) invalid("the SVD adjoint supports 1 <= k <= 64");
         const Chain ch = flatten(matrix);
+        require_stored(ch.base, "the differentiation form");
         const int64_t m = ch.base->nrow, n = ch.base->ncol;
         if (ch.scale && !ch.scale_column)
             throw Error(IRLBA_GB300_ERROR_UNSUPPORTED, "the SVD adjoint supports column scaling only");

@@ -437,6 +437,30 @@ static int64_t g_last_launches[kTNum] = {0};
 // Engine: one compute() call
 // ---------------------------------------------------------------------------
 
+// Raw product of a user-defined operator: y = A x (adjoint = false) or A^T x.
+// A device product is enqueued on `s`; a host product synchronizes `s`, runs on
+// FP64 host copies of the vectors and copies y back before returning.
+template <typename T>
+static void operator_product(const BaseMatrix& A, bool adjoint, const T* x, T* y, cudaStream_t s) {
+    const int64_t lin = adjoint ? A.nrow : A.ncol, lout = adjoint ? A.ncol : A.nrow;
+    int32_t rc = 0;
+    if (A.op.device) {
+        rc = A.op.device(A.op.user, adjoint ? 1 : 0, x, y, s);
+    } else {
+        std::vector<T> xt(static_cast<size_t>(lin));
+        CUDA_TRY(d2h_async(xt.data(), x, sizeof(T) * lin, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        std::vector<double> xd(xt.begin(), xt.end()), yd(static_cast<size_t>(lout), 0.0);
+        rc = A.op.host(A.op.user, adjoint ? 1 : 0, xd.data(), yd.data());
+        if (rc == 0) {
+            std::vector<T> yt(yd.begin(), yd.end());
+            CUDA_TRY(h2d_async(y, yt.data(), sizeof(T) * lout, s));
+            CUDA_TRY(cudaStreamSynchronize(s));
+        }
+    }
+    if (rc != 0) invalid("user-defined product failed (status " + std::to_string(rc) + ")");
+}
+
 template <typename T>
 struct Engine {
     const Chain& ch;
@@ -527,6 +551,15 @@ struct Engine {
         e.alpha = alpha;
         e.q = q;
         const T* xin = x;
+        if (A.is_operator()) {
+            if (col_scale) {
+                launch_scale_vector<T>(x, svec, ch.scale_divide, n, xtmp.as<T>(), ms);
+                xin = xtmp.as<T>();
+            }
+            operator_product<T>(A, false, xin, y, ms);
+            launch_epilogue<T>(y, m, e, &ctrl->abort, ms);
+            return;
+        }
         if (col_scale) {
             if (A.mul.dev.staged) {
                 e.iscale = svec;
@@ -556,6 +589,15 @@ struct Engine {
         e.alpha = alpha;
         e.q = q;
         const T* xin = x;
+        if (A.is_operator()) {
+            if (row_scale) {
+                launch_scale_vector<T>(x, svec, ch.scale_divide, m, xtmp.as<T>(), stream);
+                xin = xtmp.as<T>();
+            }
+            operator_product<T>(A, true, xin, y, stream);
+            launch_epilogue<T>(y, n, e, &ctrl->abort, stream);
+            return;
+        }
         if (row_scale) {
             if (A.adj.dev.staged) {
                 e.iscale = svec;
@@ -774,7 +816,9 @@ struct Engine {
         const DeviceInfo& di = device_info();
         const size_t restart_smem = di.max_smem_optin - 16384;
         // FP32 form only: the FP64 form keeps the reference's order of operations.
-        const bool overlap = std::is_same<T, float>::value;
+        // Host-side products synchronize the stream they are given, so they
+        // stay on the engine stream.
+        const bool overlap = std::is_same<T, float>::value && !A.op.host;
         if (overlap && !side) {
             CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
             CUDA_TRY(cudaEventCreateWithFlags(&ev_f, cudaEventDisableTiming));
@@ -895,10 +939,52 @@ struct Engine {
 // ---------------------------------------------------------------------------
 // Realize (dense FP64, column-major m x n) on the device.
 // ---------------------------------------------------------------------------
+template <typename T>
+__global__ void unit_vector_kernel(T* x, int64_t len, int64_t pos) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < len;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        x[i] = (i == pos) ? T(1) : T(0);
+}
+
+__global__ void transpose_kernel(const double* in, int64_t m, int64_t n, double* out);
+
+// Dense FP64 column-major realization of a user-defined operator: one product
+// per unit vector along the smaller dimension (columns A e_c, or rows A^T e_r
+// gathered into the transpose and transposed back).
+template <typename T>
+static void realize_operator(const BaseMatrix& A, double* out, cudaStream_t stream) {
+    const int64_t m = A.nrow, n = A.ncol;
+    if (m == 0 || n == 0) return;
+    const bool by_cols = n <= m;
+    const int64_t count = by_cols ? n : m, lin = by_cols ? n : m, lout = by_cols ? m : n;
+    DevBuf x(sizeof(T) * lin), y(sizeof(T) * lout), tr;
+    double* dst = out;
+    if (!by_cols) {
+        tr.alloc(sizeof(double) * m * n);
+        dst = tr.as<double>();
+    }
+    const int grid = static_cast<int>(std::min<int64_t>((std::max(lin, lout) + 255) / 256, 152 * 8));
+    for (int64_t c = 0; c < count; ++c) {
+        unit_vector_kernel<T><<<grid, 256, 0, stream>>>(x.as<T>(), lin, c); count_launch();
+        operator_product<T>(A, !by_cols, x.as<T>(), y.as<T>(), stream);
+        launch_convert<T, double>(y.as<T>(), dst + c * lout, lout, stream);
+    }
+    if (!by_cols) {
+        // dst is n x m (column r = row r of A); out = its transpose.
+        transpose_kernel<<<152 * 8, 256, 0, stream>>>(dst, n, m, out); count_launch();
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream));
+}
+
 static void realize_device(const Chain& ch, double* out, cudaStream_t stream) {
     const BaseMatrix& A = *ch.base;
     CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * A.nrow * A.ncol, stream));
-    launch_realize(A.mul.dev, out, A.nrow, 0, stream);
+    if (A.is_operator()) {
+        if (A.form == IRLBA_GB300_FORM_FP32_FP64STEPS) realize_operator<float>(A, out, stream);
+        else realize_operator<double>(A, out, stream);
+    } else {
+        launch_realize(A.mul.dev, out, A.nrow, 0, stream);
+    }
     DevBuf c, s;
     if (ch.center) c = upload(ch.center->data(), ch.center->size());
     if (ch.scale) s = upload(ch.scale->data(), ch.scale->size());
@@ -1072,6 +1158,7 @@ static std::pair<bool, int> pca_device_impl(const irlba_gb300_matrix* matrix, in
                                             double* dRot, double* dVar, double* dCenter, double* dScale,
                                             int64_t* out_number, irlba_gb300_stats* stats, cudaStream_t s) {
     if (matrix->kind != 0) invalid("pca() takes an undecorated matrix");
+    require_stored(matrix->base.get(), "pca()");
     const int64_t nr = matrix->nrow, nc = matrix->ncol;
     if (center && nr < 1) invalid("cannot center with no observations");
     if (scale && nr < 2) invalid("cannot scale with fewer than two observations");
@@ -1303,6 +1390,51 @@ irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, c
         h->ncol = ncol;
         h->form = form;
         *out = h;
+    });
+}
+
+static irlba_gb300_matrix* operator_handle(int64_t nrow, int64_t ncol, irlba_gb300_form form, UserOperator op) {
+    if (nrow < 0 || ncol < 0) invalid("matrix dimensions must be non-negative");
+    if (form != IRLBA_GB300_FORM_FP64 && form != IRLBA_GB300_FORM_FP32_FP64STEPS) invalid("unknown arithmetic form");
+    device_info();
+    auto base = std::make_shared<BaseMatrix>();
+    base->nrow = nrow;
+    base->ncol = ncol;
+    base->form = form;
+    base->store_f64 = form == IRLBA_GB300_FORM_FP64;
+    base->op = op;
+    auto* h = new irlba_gb300_matrix();
+    h->kind = 0;
+    h->base = base;
+    h->nrow = nrow;
+    h->ncol = ncol;
+    h->form = form;
+    return h;
+}
+
+irlba_gb300_status irlba_gb300_matrix_create_device_operator(int64_t nrow, int64_t ncol,
+                                                             irlba_gb300_device_product product, void* user,
+                                                             irlba_gb300_form form, irlba_gb300_matrix** out) {
+    return guarded([&]() {
+        if (!out) invalid("output handle pointer is NULL");
+        if (!product) invalid("product function must not be NULL");
+        UserOperator op;
+        op.device = product;
+        op.user = user;
+        *out = operator_handle(nrow, ncol, form, op);
+    });
+}
+
+irlba_gb300_status irlba_gb300_matrix_create_host_operator(int64_t nrow, int64_t ncol,
+                                                           irlba_gb300_host_product product, void* user,
+                                                           irlba_gb300_form form, irlba_gb300_matrix** out) {
+    return guarded([&]() {
+        if (!out) invalid("output handle pointer is NULL");
+        if (!product) invalid("product function must not be NULL");
+        UserOperator op;
+        op.host = product;
+        op.user = user;
+        *out = operator_handle(nrow, ncol, form, op);
     });
 }
 
@@ -1617,6 +1749,7 @@ irlba_gb300_status irlba_gb300_spmv_device(const irlba_gb300_matrix* matrix, int
                                            void* y, void* stream) {
     return guarded([&]() {
         if (!matrix || matrix->kind != 0) invalid("spmv_device takes an undecorated matrix");
+        require_stored(matrix->base.get(), "spmv_device");
         const BaseMatrix& A = *matrix->base;
         const DirPlan& p = adjoint ? A.adj : A.mul;
         cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1647,6 +1780,7 @@ irlba_gb300_status irlba_gb300_matrix_layout(const irlba_gb300_matrix* matrix, i
                                              int32_t* panels_adj) {
     return guarded([&]() {
         if (!matrix || matrix->kind != 0) invalid("matrix_layout takes an undecorated matrix");
+        require_stored(matrix->base.get(), "matrix_layout");
         const BaseMatrix& A = *matrix->base;
         *nnz = A.mul.dev.nnz;
         *value_bytes = A.store_f64 ? 8 : 4;

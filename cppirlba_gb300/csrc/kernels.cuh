@@ -60,6 +60,11 @@ template <typename T>
 void launch_spmv(const DirPlanDev& p, const T* x, T* y, T* partial, const Epilogue<T>& e, const int32_t* abort,
                  cudaStream_t stream);
 
+// The epilogue alone, applied in place to y (the raw product of a user-defined
+// operator); a no-op when e has no beta, oscale or alpha.
+template <typename T>
+void launch_epilogue(T* y, int64_t nrows, const Epilogue<T>& e, const int32_t* abort, cudaStream_t stream);
+
 // Launch configuration helpers (dynamic shared-memory limits, occupancy, grids).
 cudaError_t spmv_configure(size_t max_smem);
 int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group);

@@ -16,12 +16,23 @@ struct DirPlan {
     DevBuf segptr, idx, val, block_seg;
 };
 
+// A user-defined operator in place of the stored gather plans: its products are
+// the caller's functions (device code on the engine's stream, or host code with
+// the vectors copied around each call).
+struct UserOperator {
+    irlba_gb300_device_product device = nullptr;
+    irlba_gb300_host_product host = nullptr;
+    void* user = nullptr;
+};
+
 struct BaseMatrix {
     int64_t nrow = 0, ncol = 0;
     irlba_gb300_form form = IRLBA_GB300_FORM_FP64;
     bool store_f64 = true;
     DirPlan mul;  // rows = nrow, x = ncol
     DirPlan adj;  // rows = ncol, x = nrow
+    UserOperator op;
+    bool is_operator() const { return op.device != nullptr || op.host != nullptr; }
 };
 
 }  // namespace irlba_gb300
@@ -73,6 +84,14 @@ inline Chain flatten(const irlba_gb300_matrix* m) {
     // decos[0] is outermost.
     if (ncenter == 1 && nscale == 1) ch.center_outer = (decos[0]->kind == 1) ? 1 : 0;
     return ch;
+}
+
+// Paths that read the stored entries (column statistics, SpMM, SDDMM, the raw
+// SpMV entry point) reject user-defined operators.
+inline void require_stored(const BaseMatrix* b, const char* what) {
+    if (b->is_operator())
+        throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
+                    std::string(what) + " needs a stored (sparse or dense) matrix, not a user-defined operator");
 }
 
 }  // namespace irlba_gb300

@@ -127,6 +127,18 @@ __global__ void panel_reduce_kernel(const T* __restrict__ partial, int32_t npane
     }
 }
 
+// The epilogue alone, in place, over the raw product of a user-defined operator.
+template <typename T>
+__global__ void epilogue_kernel(T* y, int64_t nrows, const Epilogue<T> e, const int32_t* abort) {
+    if (*abort) return;
+    EpiVals<T> ev;
+    ev.beta = e.beta ? static_cast<T>(*e.beta) : T(0);
+    ev.alpha = e.alpha ? static_cast<T>(*e.alpha) : T(0);
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < nrows;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        y[r] = apply_epilogue(y[r], r, e, ev);
+}
+
 template <typename T>
 __global__ void scale_vector_kernel(const T* __restrict__ x, const T* __restrict__ s, int32_t divide, int64_t n,
                                     T* __restrict__ out) {
@@ -182,6 +194,14 @@ void launch_spmv(const DirPlanDev& p, const T* x, T* y, T* partial, const Epilog
 }
 
 template <typename T>
+void launch_epilogue(T* y, int64_t nrows, const Epilogue<T>& e, const int32_t* abort, cudaStream_t stream) {
+    if (nrows == 0) return;
+    if (!e.beta && !e.oscale && !e.alpha) return;
+    epilogue_kernel<T><<<grid_for(nrows, 256, 152 * 16), 256, 0, stream>>>(y, nrows, e, abort);
+    count_launch();
+}
+
+template <typename T>
 void launch_scale_vector(const T* x, const T* s, int32_t divide, int64_t n, T* out, cudaStream_t stream) {
     if (n == 0) return;
     scale_vector_kernel<T><<<grid_for(n, 256, 152 * 16), 256, 0, stream>>>(x, s, divide, n, out);
@@ -218,6 +238,8 @@ template void launch_spmv<float>(const DirPlanDev&, const float*, float*, float*
                                  const int32_t*, cudaStream_t);
 template void launch_spmv<double>(const DirPlanDev&, const double*, double*, double*, const Epilogue<double>&,
                                   const int32_t*, cudaStream_t);
+template void launch_epilogue<float>(float*, int64_t, const Epilogue<float>&, const int32_t*, cudaStream_t);
+template void launch_epilogue<double>(double*, int64_t, const Epilogue<double>&, const int32_t*, cudaStream_t);
 template void launch_scale_vector<float>(const float*, const float*, int32_t, int64_t, float*, cudaStream_t);
 template void launch_scale_vector<double>(const double*, const double*, int32_t, int64_t, double*, cudaStream_t);
 

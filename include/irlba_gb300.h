@@ -10,6 +10,7 @@
  *   matrix handles      <- irlba::Matrix and subclasses   include/irlba/Matrix/interface.hpp:141-223
  *   sparse create       <- irlba::ParallelSparseMatrix    include/irlba/Matrix/sparse.hpp:469-471
  *   dense create        <- irlba::SimpleMatrix            include/irlba/Matrix/simple.hpp:124-178
+ *   operator create     <- a user subclass of irlba::Matrix include/irlba/Matrix/interface.hpp:141-223
  *   center              <- irlba::CenteredMatrix          include/irlba/Matrix/centered.hpp:139-204
  *   scale               <- irlba::ScaledMatrix            include/irlba/Matrix/scaled.hpp:195-268
  *   multiply            <- Workspace::multiply            include/irlba/Matrix/interface.hpp:49
@@ -121,6 +122,38 @@ irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, c
 
 /* CenteredMatrix(inner, center) (centered.hpp:152): column centring, center has
  * length ncol. The inner handle must outlive the new one. */
+/* A user-defined matrix: the counterpart of a user subclass of irlba::Matrix
+ * (Matrix/interface.hpp:141-223), e.g. a residual matrix that is never stored.
+ * The engine runs its whole IRLBA loop (and any CenteredMatrix / ScaledMatrix
+ * over it, fused into one elementwise pass after each product) on the device
+ * and calls `product` for each Workspace::multiply (adjoint = 0: y = A x, x of
+ * length ncol, y of length nrow) and AdjointWorkspace::multiply (adjoint = 1:
+ * y = A^T x). Both functions return 0 on success; any other value makes the
+ * running call fail with IRLBA_GB300_ERROR_INVALID_ARGUMENT ("user-defined
+ * product failed"). `user` is passed through untouched. Products are issued
+ * one at a time; `y` arrives dirty and must be fully overwritten, and `x` must
+ * not be modified. pca() (which needs the stored columns for its statistics),
+ * the differentiation form and irlba_gb300_spmv_device reject these handles. */
+
+/* Device product: x and y are device vectors of the form's type (double for
+ * IRLBA_GB300_FORM_FP64, float for IRLBA_GB300_FORM_FP32_FP64STEPS). The
+ * function enqueues its work on `stream` (a cudaStream_t) and returns without
+ * waiting for it; it may be called on more than one of the engine's streams,
+ * always ordered after the producer of x and before the consumer of y. */
+typedef int32_t (*irlba_gb300_device_product)(void* user, int32_t adjoint, const void* x, void* y, void* stream);
+
+/* Host product: x and y are FP64 host vectors; the engine copies x out of and
+ * y back into device memory around each call (one synchronization per
+ * product: correct but not fast). */
+typedef int32_t (*irlba_gb300_host_product)(void* user, int32_t adjoint, const double* x, double* y);
+
+irlba_gb300_status irlba_gb300_matrix_create_device_operator(int64_t nrow, int64_t ncol,
+                                                             irlba_gb300_device_product product, void* user,
+                                                             irlba_gb300_form form, irlba_gb300_matrix** out);
+irlba_gb300_status irlba_gb300_matrix_create_host_operator(int64_t nrow, int64_t ncol,
+                                                           irlba_gb300_host_product product, void* user,
+                                                           irlba_gb300_form form, irlba_gb300_matrix** out);
+
 irlba_gb300_status irlba_gb300_matrix_center(const irlba_gb300_matrix* inner, const double* center,
                                              irlba_gb300_matrix** out);
 

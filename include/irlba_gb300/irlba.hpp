@@ -23,6 +23,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <optional>
 #include <random>
@@ -68,6 +69,77 @@ struct is_row_major<T, std::void_t<decltype(T::IsRowMajor)>> : std::integral_con
 
 template <class P>
 auto& deref(const P& p) { return *p; }
+
+// Engine handle of a matrix, or NULL for one the engine cannot run directly
+// (a user's own Matrix subclass, or a type without gpu_handle()).
+template <class M, class = void>
+struct has_gpu_handle : std::false_type {};
+template <class M>
+struct has_gpu_handle<M, std::void_t<decltype(std::declval<const M&>().gpu_handle())>> : std::true_type {};
+template <class M>
+const irlba_gb300_matrix* handle_of(const M& m) {
+    if constexpr (has_gpu_handle<M>::value) return m.gpu_handle();
+    else return nullptr;
+}
+
+// Products of a matrix without an engine handle, run on the host through its
+// own workspaces (Workspace::multiply / AdjointWorkspace::multiply,
+// Matrix/interface.hpp:49,87) for the engine's host-operator path: the IRLBA
+// loop stays on the device and each product copies its vectors across.
+template <class Matrix_, class EigenVector_>
+class HostProducts {
+public:
+    explicit HostProducts(const Matrix_& m) : my_matrix(m) {}
+    static int32_t call(void* self, int32_t adjoint, const double* x, double* y) {
+        auto* me = static_cast<HostProducts*>(self);
+        try {
+            me->run(adjoint != 0, x, y);
+            return 0;
+        } catch (const std::exception& e) {
+            me->error = e.what();
+        } catch (...) {
+            me->error = "user-defined product threw";
+        }
+        return 1;
+    }
+    std::string error;
+
+private:
+    void run(bool adjoint, const double* x, double* y) {
+        const Index nin = adjoint ? my_matrix.rows() : my_matrix.cols();
+        const Index nout = adjoint ? my_matrix.cols() : my_matrix.rows();
+        my_in.resize(nin);
+        for (Index i = 0; i < nin; ++i) my_in.data()[i] = x[i];
+        my_out.resize(nout);
+        if (adjoint) {
+            if (!my_adj) my_adj = my_matrix.new_known_adjoint_workspace();
+            my_adj->multiply(my_in, my_out);
+        } else {
+            if (!my_mul) my_mul = my_matrix.new_known_workspace();
+            my_mul->multiply(my_in, my_out);
+        }
+        for (Index i = 0; i < nout; ++i) y[i] = static_cast<double>(my_out.data()[i]);
+    }
+    const Matrix_& my_matrix;
+    decltype(std::declval<const Matrix_&>().new_known_workspace()) my_mul;
+    decltype(std::declval<const Matrix_&>().new_known_adjoint_workspace()) my_adj;
+    EigenVector_ my_in, my_out;
+};
+
+// Engine handle of `m`: its own, or a host operator over its workspaces (kept
+// alive by `products` and `op`).
+template <class EigenVector_, class Matrix_>
+const irlba_gb300_matrix* handle_or_host_operator(const Matrix_& m, std::shared_ptr<void>& products, Handle& op) {
+    const irlba_gb300_matrix* h = handle_of(m);
+    if (h) return h;
+    auto p = std::make_shared<HostProducts<Matrix_, EigenVector_>>(m);
+    irlba_gb300_matrix* raw = nullptr;
+    check(irlba_gb300_matrix_create_host_operator(m.rows(), m.cols(), &HostProducts<Matrix_, EigenVector_>::call,
+                                                  p.get(), default_form(), &raw));
+    op = adopt(raw);
+    products = p;
+    return raw;
+}
 
 }  // namespace gpu
 
@@ -237,6 +309,39 @@ protected:
     Index my_nrow = 0, my_ncol = 0;
 };
 
+// A user-defined matrix whose products run on the device, e.g. a residual
+// matrix that is never stored: the GPU form of a user's own Matrix subclass
+// (Matrix/interface.hpp:141-223). product(adjoint, x, y, stream) enqueues
+// y = A x (adjoint false; x of length cols()) or y = A^T x on the cudaStream_t
+// `stream` and returns; x and y are device vectors of double (FP64 form) or
+// float (FP32 form, see set_form()). A product that throws fails the running
+// call.
+template <class EigenVector_, class EigenMatrix_>
+class DeviceMatrix final : public HandleMatrix<EigenVector_, EigenMatrix_> {
+public:
+    typedef std::function<void(bool adjoint, const void* x, void* y, void* stream)> Product;
+    DeviceMatrix(Index nrow, Index ncol, Product product) : my_product(new Product(std::move(product))) {
+        irlba_gb300_matrix* h = nullptr;
+        check(irlba_gb300_matrix_create_device_operator(nrow, ncol, &DeviceMatrix::call, my_product.get(),
+                                                        default_form(), &h));
+        this->my_handle = adopt(h);
+        this->my_nrow = nrow;
+        this->my_ncol = ncol;
+    }
+    ~DeviceMatrix() { this->my_handle.reset(); }
+
+private:
+    static int32_t call(void* user, int32_t adjoint, const void* x, void* y, void* stream) {
+        try {
+            (*static_cast<Product*>(user))(adjoint != 0, x, y, stream);
+            return 0;
+        } catch (...) {
+            return 1;
+        }
+    }
+    std::unique_ptr<Product> my_product;
+};
+
 }  // namespace gpu
 
 // SimpleMatrix over a dense matrix (simple.hpp:124-178). The data are copied
@@ -329,8 +434,7 @@ class CenteredMatrix final : public gpu::HandleMatrix<EigenVector_, EigenMatrix_
 public:
     CenteredMatrix(MatrixPointer_ matrix, CenterPointer_ center) : my_matrix(std::move(matrix)), my_center(std::move(center)) {
         const auto& inner = gpu::deref(my_matrix);
-        const irlba_gb300_matrix* ih = inner.gpu_handle();
-        if (!ih) throw std::runtime_error("CenteredMatrix on the GPU engine needs an engine-backed inner matrix");
+        const irlba_gb300_matrix* ih = gpu::handle_or_host_operator<EigenVector_>(inner, my_products, my_inner_op);
         const auto& c = gpu::deref(my_center);
         std::vector<double> cv(c.data(), c.data() + c.size());
         if (static_cast<Index>(cv.size()) != inner.cols()) throw std::runtime_error("center has the wrong length");
@@ -341,9 +445,13 @@ public:
         this->my_ncol = inner.cols();
     }
 
+    ~CenteredMatrix() { this->my_handle.reset(); }
+
 private:
     MatrixPointer_ my_matrix;
     CenterPointer_ my_center;
+    std::shared_ptr<void> my_products;  // host products of an inner matrix without an engine handle
+    gpu::Handle my_inner_op;
 };
 
 // ScaledMatrix (scaled.hpp:195-268).
@@ -354,8 +462,7 @@ public:
     ScaledMatrix(MatrixPointer_ matrix, ScalePointer_ scale, bool column, bool divide)
         : my_matrix(std::move(matrix)), my_scale(std::move(scale)) {
         const auto& inner = gpu::deref(my_matrix);
-        const irlba_gb300_matrix* ih = inner.gpu_handle();
-        if (!ih) throw std::runtime_error("ScaledMatrix on the GPU engine needs an engine-backed inner matrix");
+        const irlba_gb300_matrix* ih = gpu::handle_or_host_operator<EigenVector_>(inner, my_products, my_inner_op);
         const auto& s = gpu::deref(my_scale);
         std::vector<double> sv(s.data(), s.data() + s.size());
         if (static_cast<Index>(sv.size()) != (column ? inner.cols() : inner.rows()))
@@ -367,9 +474,13 @@ public:
         this->my_ncol = inner.cols();
     }
 
+    ~ScaledMatrix() { this->my_handle.reset(); }
+
 private:
     MatrixPointer_ my_matrix;
     ScalePointer_ my_scale;
+    std::shared_ptr<void> my_products;  // host products of an inner matrix without an engine handle
+    gpu::Handle my_inner_op;
 };
 
 // ---------------------------------------------------------------------------
@@ -392,8 +503,11 @@ void fill_vector(EigenVector_& out, const std::vector<double>& v, Index n) {
 template <class Matrix_, class EigenMatrix_, class EigenVector_>
 std::pair<bool, int> compute(const Matrix_& matrix, Index number, EigenMatrix_& outU, EigenMatrix_& outV,
                              EigenVector_& outD, const Options<EigenVector_>& options) {
-    const irlba_gb300_matrix* h = matrix.gpu_handle();
-    if (!h) throw std::runtime_error("the GPU engine runs matrices built from its own Matrix types");
+    // A matrix without an engine handle (a user's own Matrix subclass) runs
+    // with the loop on the device and its products called on the host.
+    std::shared_ptr<void> products;
+    gpu::Handle host_op;
+    const irlba_gb300_matrix* h = gpu::handle_or_host_operator<EigenVector_>(matrix, products, host_op);
     const Index nr = matrix.rows(), nc = matrix.cols();
     const Index cap = std::max<Index>(std::min<Index>(number, std::min(nr, nc)), 0);
     std::vector<double> U(static_cast<size_t>(nr * cap)), V(static_cast<size_t>(nc * cap)), D(cap > 0 ? cap : 1);
@@ -401,7 +515,13 @@ std::pair<bool, int> compute(const Matrix_& matrix, Index number, EigenMatrix_& 
     irlba_gb300_options o = gpu::to_c(options, init);
     int64_t num = 0;
     int32_t conv = 0, iters = 0;
-    gpu::check(irlba_gb300_compute(h, number, &o, U.data(), V.data(), D.data(), &num, &conv, &iters, nullptr));
+    const irlba_gb300_status st =
+        irlba_gb300_compute(h, number, &o, U.data(), V.data(), D.data(), &num, &conv, &iters, nullptr);
+    if (st != IRLBA_GB300_OK && products) {
+        const std::string& why = static_cast<gpu::HostProducts<Matrix_, EigenVector_>*>(products.get())->error;
+        if (!why.empty()) throw std::runtime_error(why);
+    }
+    gpu::check(st);
     gpu::fill_matrix(outU, nr, num, U);
     gpu::fill_matrix(outV, nc, num, V);
     gpu::fill_vector(outD, D, num);

@@ -1,10 +1,13 @@
 // Exercises the header-style drop-in (include/irlba_gb300/irlba.hpp) the way a
 // CppIrlba user would: irlba::compute / compute_simple / pca over SimpleMatrix,
-// ParallelSparseMatrix and the Centered/Scaled decorators. Prints inputs and
+// ParallelSparseMatrix, the Centered/Scaled decorators, a user's own Matrix
+// subclass and a gpu::DeviceMatrix. Prints inputs and
 // outputs as JSON for tests/test_gpu_dropin.py to check against the oracle.
 #include <cmath>
 #include <cstdio>
 #include <cstdint>
+#include <memory>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -34,6 +37,52 @@ struct Mat {
     void resize(std::ptrdiff_t r, std::ptrdiff_t c) { nr = r; nc = c; v.assign(r * c, 0.0); }
     double& operator()(std::ptrdiff_t r, std::ptrdiff_t c) { return v[c * nr + r]; }
     double operator()(std::ptrdiff_t r, std::ptrdiff_t c) const { return v[c * nr + r]; }
+};
+
+// A caller's own Matrix subclass (Matrix/interface.hpp:141-223) with products
+// written by hand on the host; `fail` makes its multiply throw.
+class UserDense final : public irlba::Matrix<Vec, Mat> {
+public:
+    UserDense(const Mat* a, bool fail = false) : my_a(a), my_fail(fail) {}
+    irlba::Index rows() const { return my_a->rows(); }
+    irlba::Index cols() const { return my_a->cols(); }
+
+    struct Mul final : public irlba::Workspace<Vec> {
+        const Mat* a;
+        bool fail;
+        Mul(const Mat* a_, bool f) : a(a_), fail(f) {}
+        void multiply(const Vec& right, Vec& out) {
+            if (fail) throw std::runtime_error("residual model is not fitted");
+            for (std::ptrdiff_t r = 0; r < a->rows(); ++r) {
+                double s = 0;
+                for (std::ptrdiff_t c = 0; c < a->cols(); ++c) s += (*a)(r, c) * right.v[c];
+                out.v[r] = s;
+            }
+        }
+    };
+    struct Adj final : public irlba::AdjointWorkspace<Vec> {
+        const Mat* a;
+        explicit Adj(const Mat* a_) : a(a_) {}
+        void multiply(const Vec& right, Vec& out) {
+            for (std::ptrdiff_t c = 0; c < a->cols(); ++c) {
+                double s = 0;
+                for (std::ptrdiff_t r = 0; r < a->rows(); ++r) s += (*a)(r, c) * right.v[r];
+                out.v[c] = s;
+            }
+        }
+    };
+    struct Real final : public irlba::RealizeWorkspace<Mat> {
+        const Mat* a;
+        explicit Real(const Mat* a_) : a(a_) {}
+        const Mat& realize(Mat&) { return *a; }
+    };
+    std::unique_ptr<irlba::Workspace<Vec>> new_workspace() const { return std::make_unique<Mul>(my_a, my_fail); }
+    std::unique_ptr<irlba::AdjointWorkspace<Vec>> new_adjoint_workspace() const { return std::make_unique<Adj>(my_a); }
+    std::unique_ptr<irlba::RealizeWorkspace<Mat>> new_realize_workspace() const { return std::make_unique<Real>(my_a); }
+
+private:
+    const Mat* my_a;
+    bool my_fail;
 };
 
 static uint64_t lcg = 88172645463325252ull;
@@ -115,6 +164,34 @@ int main() {
     Vec out(nr);
     w->multiply(init, out);
     dump_vec("chain_multiply_init", out.data(), nr);
+
+    // A caller's own Matrix subclass: the loop on the device, products on the host.
+    UserDense user(&A);
+    auto res4 = irlba::compute<Mat, Vec>(user, 6, opt);
+    dump_vec("user_D", res4.D.data(), res4.D.size());
+    std::printf("\"user_iterations\": %d,\n", res4.iterations);
+    irlba::CenteredMatrix<Vec, Mat> ucen(&user, &center);
+    auto res5 = irlba::compute<Mat, Vec>(ucen, 4, opt);
+    dump_vec("user_centered_D", res5.D.data(), res5.D.size());
+    std::printf("\"user_centered_iterations\": %d,\n", res5.iterations);
+    std::string user_msg;
+    try {
+        UserDense broken(&A, true);
+        irlba::compute<Mat, Vec>(broken, 6, opt);
+    } catch (const std::exception& e) {
+        user_msg = e.what();
+    }
+    std::printf("\"user_error_message\": \"%s\",\n", user_msg.c_str());
+
+    // A matrix whose products are device code on the engine's stream (here the
+    // engine's own SpMV of the sparse matrix, through its raw entry point).
+    const irlba_gb300_matrix* sph = sp.gpu_handle();
+    irlba::gpu::DeviceMatrix<Vec, Mat> dev(nr, nc, [sph](bool adjoint, const void* in, void* out, void* stream) {
+        irlba::gpu::check(irlba_gb300_spmv_device(sph, adjoint ? 1 : 0, in, out, stream));
+    });
+    auto res6 = irlba::compute<Mat, Vec>(dev, 4, opt);
+    dump_vec("device_D", res6.D.data(), res6.D.size());
+    std::printf("\"device_iterations\": %d,\n", res6.iterations);
 
     // An error with the reference's message (compute.hpp:156).
     std::string msg;

@@ -69,3 +69,19 @@ def test_datagen_deterministic_and_dense_enough():
     inp = datagen.SparseInput(4000, 50, ptr, idx, val, column_major=True)
     inp2 = datagen.SparseInput(4000, 50, tp, ti, tv, column_major=False)
     np.testing.assert_array_equal(inp.to_dense(), inp2.to_dense())
+
+
+def test_operator_constructors_check_arguments_without_gpu():
+    lib = eng.load_library()
+    h = ctypes.c_void_p()
+    for fn in (lib.irlba_gb300_matrix_create_host_operator, lib.irlba_gb300_matrix_create_device_operator):
+        assert fn(10, 5, None, None, eng.FORM_FP64, ctypes.byref(h)) == eng.ERROR_INVALID_ARGUMENT
+        assert "must not be NULL" in lib.irlba_gb300_last_error().decode()
+    if eng.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(eng.IrlbaError) as e:
+        eng.OperatorMatrix(10, 5, lambda x: np.zeros(10), lambda y: np.zeros(5))
+    assert e.value.status == eng.ERROR_CUDA
+    with pytest.raises(eng.IrlbaError) as e:
+        eng.DeviceOperatorMatrix(10, 5, lambda adjoint, x, y, stream: None)
+    assert e.value.status == eng.ERROR_CUDA

@@ -52,3 +52,25 @@ def test_dropin_decorated_sparse(dropin_output, oracle_mod):
     assert d["chain_iterations"] == orc["iterations"]
     np.testing.assert_allclose(d["chain_multiply_init"], oracle_mod.multiply(spec, init), rtol=1e-12, atol=1e-12)
     assert "cannot be greater than" in d["error_message"]
+
+
+def test_dropin_user_matrices(dropin_output, oracle_mod):
+    """A caller's own irlba::Matrix subclass (host products through its
+    workspaces), a CenteredMatrix over it, and a gpu::DeviceMatrix whose
+    products are device code, each against the oracle."""
+    d = dropin_output
+    nr, nc = 120, 70
+    A = np.array(d["A_colmajor"]).reshape(nc, nr).T
+    init = np.array(d["init"])
+    orc = oracle_mod.compute(oracle_mod.Spec.dense(A), 6, oracle_mod.options(initial=init))
+    np.testing.assert_allclose(d["user_D"], orc["D"], rtol=1e-10)
+    assert d["user_iterations"] == orc["iterations"]
+    cen = oracle_mod.compute(oracle_mod.Spec.dense(A, center=np.array(d["center"])), 4,
+                             oracle_mod.options(initial=init))
+    np.testing.assert_allclose(d["user_centered_D"], cen["D"], rtol=1e-10)
+    assert d["user_centered_iterations"] == cen["iterations"]
+    assert "residual model is not fitted" in d["user_error_message"]
+    x, i, p = np.array(d["sparse_x"]), np.array(d["sparse_i"], dtype=np.int32), np.array(d["sparse_p"], dtype=np.int64)
+    sp = oracle_mod.compute(oracle_mod.Spec.sparse(nr, nc, x, i, p, True, 1), 4, oracle_mod.options(initial=init))
+    np.testing.assert_allclose(d["device_D"], sp["D"], rtol=1e-10)
+    assert d["device_iterations"] == sp["iterations"]
