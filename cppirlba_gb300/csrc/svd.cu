@@ -152,6 +152,9 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kClusterT
 
     const int n2 = n + (n & 1), half = n2 / 2;
     const double thresh = 2.220446049250313e-16 * static_cast<double>(n);
+    // The skip test |g| <= thresh sqrt(a b), squared: one FP64 square root less
+    // on each round's dependent chain (a, b >= 0).
+    const double thresh2 = thresh * thresh;
     int buf = 0;
     int sweep = 0;
     for (; sweep < kMaxSweeps; ++sweep) {
@@ -197,7 +200,7 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kClusterT
                     double g = 0;
                     for (int r = 0; r < kClusterCTAs; ++r) g += cl.map_shared_rank(part[buf], r)[slot];
                     const double av = nrm[p], bv = nrm[q];
-                    if (!(g == 0.0 || fabs(g) <= thresh * sqrt(av * bv))) {
+                    if (!(g == 0.0 || g * g <= thresh2 * (av * bv))) {
                         const double d = bv - av;
                         const double t = (d >= 0 ? 1.0 : -1.0) * (g >= 0 ? 1.0 : -1.0) * fabs(2.0 * g) /
                                          (fabs(d) + sqrt(d * d + 4.0 * g * g));

@@ -20,7 +20,9 @@ namespace irlba_gb300 {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kDotRows = 1024;     // rows per CTA of the GEMV-transpose pass
+constexpr int kDotRows = 1024;     // rows of v staged per sub-chunk of the GEMV-transpose pass
+constexpr int kDotUnit = 256;      // granularity of its row ranges
+constexpr int kDotMaxRanges = 1216;  // upper bound of its row ranges (gridDim.x)
 constexpr int kMaxCols = 1024;     // basis columns held in shared memory
 
 int grid_for(int64_t n, int threads, int cap) {
@@ -33,9 +35,16 @@ int grid_for(int64_t n, int threads, int cap) {
 // ---------------------------------------------------------------------------
 // t = Q[:, :c]^T v
 // ---------------------------------------------------------------------------
-// Grid: x = chunks of kDotRows rows, y = groups of (threads / 32) columns; one
-// warp per (chunk, column). The last CTA reduces the per-chunk partials with one
-// warp per column (lane-strided over chunks, then a shuffle tree): fixed order.
+// Grid: x = row ranges, y = groups of (threads / 32) columns; one warp per
+// (range, column). gridDim.x is sized so the whole grid is one wave of resident
+// CTAs, and each range is a balanced run of 256-row units processed in
+// sub-chunks of kDotRows rows (v staged in shared memory per sub-chunk). Lanes
+// keep their FP64 accumulators across the whole range, so the FP64 shuffle
+// reduction runs once per (range, column): on GB300, whose FP64 rate is about
+// 1/60 of its FP32 rate, per-sub-chunk reductions made the FP64 pipe a
+// co-bottleneck of this memory-bound pass. The last CTA reduces the per-range
+// partials with one warp per column (lane-strided, then a shuffle tree): the
+// summation order is fixed, so results are bit-reproducible.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) cgs_dot_kernel(const T* __restrict__ Q, int64_t L, int64_t ldq, int32_t c,
                                                            const T* __restrict__ v, double* __restrict__ part,
@@ -43,31 +52,36 @@ __global__ void __launch_bounds__(kThreads) cgs_dot_kernel(const T* __restrict__
     __shared__ T vs[kDotRows];
     __shared__ bool is_last;
     if (ctrl->abort) return;
-    const int64_t r0 = static_cast<int64_t>(blockIdx.x) * kDotRows;
-    const int rows = static_cast<int>((L - r0 < kDotRows ? L - r0 : static_cast<int64_t>(kDotRows)));
-    for (int i = threadIdx.x; i < rows; i += blockDim.x) vs[i] = v[r0 + i];
-    __syncthreads();
+    const int64_t units = (L + kDotUnit - 1) / kDotUnit;
+    const int64_t u0 = units * blockIdx.x / gridDim.x, u1 = units * (blockIdx.x + 1) / gridDim.x;
+    const int64_t rbeg = u0 * kDotUnit, rend = (u1 * kDotUnit < L) ? u1 * kDotUnit : L;
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int j = static_cast<int>(blockIdx.y) * nw + warp;
-    if (j < c) {
-        const T* __restrict__ q = Q + j * ldq + r0;
-        double acc = 0;
-        int i = lane;
-        for (; i + 7 * 32 < rows; i += 8 * 32) {
-            T s = 0;
+    double acc = 0;
+    for (int64_t r0 = rbeg; r0 < rend; r0 += kDotRows) {
+        const int rows = static_cast<int>((rend - r0 < kDotRows ? rend - r0 : static_cast<int64_t>(kDotRows)));
+        __syncthreads();  // the previous sub-chunk's readers are done with vs
+        for (int i = threadIdx.x; i < rows; i += blockDim.x) vs[i] = v[r0 + i];
+        __syncthreads();
+        if (j < c) {
+            const T* __restrict__ q = Q + j * ldq + r0;
+            int i = lane;
+            for (; i + 7 * 32 < rows; i += 8 * 32) {
+                T s = 0;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) s += q[i + u * 32] * vs[i + u * 32];
-            acc += static_cast<double>(s);
+                for (int u = 0; u < 8; ++u) s += q[i + u * 32] * vs[i + u * 32];
+                acc += static_cast<double>(s);
+            }
+            {
+                T s = 0;
+                for (; i < rows; i += 32) s += q[i] * vs[i];
+                acc += static_cast<double>(s);
+            }
         }
-        {
-            T s = 0;
-            for (; i < rows; i += 32) s += q[i] * vs[i];
-            acc += static_cast<double>(s);
-        }
-        acc = warp_sum(acc);
-        if (lane == 0) part[static_cast<int64_t>(blockIdx.x) * c + j] = acc;
     }
+    acc = warp_sum(acc);
+    if (j < c && lane == 0) part[static_cast<int64_t>(blockIdx.x) * c + j] = acc;
 
     if (last_block(&ctrl->ticket[kTicketDot], &is_last)) {
         const int chunks = static_cast<int>(gridDim.x);
@@ -482,17 +496,48 @@ __global__ void feature_finalize_kernel(int64_t nf, int64_t nobs, int32_t center
 
 }  // namespace
 
+// Row ranges of the GEMV-transpose pass for c columns: one wave of resident
+// CTAs over all column groups, at most one range per 256-row unit and at most
+// kDotMaxRanges (the bound cgs_dot_grid() reports for scratch sizing).
+template <typename T>
+static int cgs_dot_ranges(int64_t L, int32_t c) {
+    static const int per_sm = [] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, cgs_dot_kernel<T>, kThreads, 0) != cudaSuccess || b < 1) {
+            cudaGetLastError();
+            b = 1;
+        }
+        return b;
+    }();
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms < 1) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    const int groups = (c + kThreads / 32 - 1) / (kThreads / 32);
+    int64_t g = static_cast<int64_t>(sms) * per_sm / groups;
+    const int64_t units = (L + kDotUnit - 1) / kDotUnit;
+    if (g > units) g = units;
+    if (g > kDotMaxRanges) g = kDotMaxRanges;
+    if (g < 1) g = 1;
+    return static_cast<int>(g);
+}
+
 template <typename T>
 void launch_cgs_dot(const T* Q, int64_t L, int64_t ldq, int32_t c, const T* v, double* part, double* t, Ctrl* ctrl,
                     cudaStream_t stream) {
     if (c <= 0 || L == 0) return;
-    const dim3 grid(static_cast<unsigned>((L + kDotRows - 1) / kDotRows),
+    const dim3 grid(static_cast<unsigned>(cgs_dot_ranges<T>(L, c)),
                     static_cast<unsigned>((c + kThreads / 32 - 1) / (kThreads / 32)));
     cgs_dot_kernel<T><<<grid, kThreads, 0, stream>>>(Q, L, ldq, c, v, part, t, ctrl); count_launch();
 }
 
 int cgs_update_grid(int64_t L) { return grid_for(L, kThreads, 152 * 8); }
-int cgs_dot_grid(int64_t L) { return static_cast<int>((L + kDotRows - 1) / kDotRows); }
+int cgs_dot_grid(int64_t L) {
+    const int64_t units = (L + kDotUnit - 1) / kDotUnit;
+    return static_cast<int>(units < kDotMaxRanges ? units : kDotMaxRanges);
+}
 
 template <typename T>
 void launch_cgs_update(const T* Q, int64_t L, int64_t ldq, int32_t c, const double* t, T* v, double* part,

@@ -120,8 +120,6 @@ irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, c
                                                    int32_t row_major, irlba_gb300_form form,
                                                    irlba_gb300_matrix** out);
 
-/* CenteredMatrix(inner, center) (centered.hpp:152): column centring, center has
- * length ncol. The inner handle must outlive the new one. */
 /* A user-defined matrix: the counterpart of a user subclass of irlba::Matrix
  * (Matrix/interface.hpp:141-223), e.g. a residual matrix that is never stored.
  * The engine runs its whole IRLBA loop (and any CenteredMatrix / ScaledMatrix
@@ -154,6 +152,8 @@ irlba_gb300_status irlba_gb300_matrix_create_host_operator(int64_t nrow, int64_t
                                                            irlba_gb300_host_product product, void* user,
                                                            irlba_gb300_form form, irlba_gb300_matrix** out);
 
+/* CenteredMatrix(inner, center) (centered.hpp:152): column centring, center has
+ * length ncol. The inner handle must outlive the new one. */
 irlba_gb300_status irlba_gb300_matrix_center(const irlba_gb300_matrix* inner, const double* center,
                                              irlba_gb300_matrix** out);
 
@@ -208,7 +208,7 @@ irlba_gb300_status irlba_gb300_orthogonalize_vector_device(const double* Q, int6
  * fixed 1 MiB device array per GPU, held until the process exits; the first
  * call on a device looks up its address (make it before any stream capture).
  * Calls that overlap on the GPU race on the shared scratch. Needs
- * 128 + round_up(ncols, 32) + max(ceil(L / 1024) * ncols, min(ceil(L / 256), 1216))
+ * 128 + round_up(ncols, 32) + min(ceil(L / 256), 1216) * max(ncols, 1)
  * <= 131072 doubles; larger requests return IRLBA_GB300_ERROR_INVALID_ARGUMENT. */
 irlba_gb300_status irlba_gb300_orthogonalize_vector_device_noalloc(const double* Q, int64_t L, int64_t ldq,
                                                                    int64_t ncols, double* vec, void* stream);
