@@ -9,7 +9,8 @@
 //    output assembly (compute.hpp:298-305);
 //  * realization and PCA column statistics (pca.hpp:85-109).
 // Coefficients and norms accumulate in FP64 in both precision forms: in the FP32
-// form each lane sums 8 FP32 products before adding them to an FP64 total.
+// form each lane sums 16 FP32 products (the dot pass) or one row's products (the
+// update pass) before adding them to an FP64 total.
 
 #include <type_traits>
 
@@ -67,10 +68,13 @@ __global__ void __launch_bounds__(kThreads) cgs_dot_kernel(const T* __restrict__
         if (j < c) {
             const T* __restrict__ q = Q + j * ldq + r0;
             int i = lane;
-            for (; i + 7 * 32 < rows; i += 8 * 32) {
+            // 16-product partials: 16 loads in flight per lane and one
+            // conversion and FP64 add per 16 products (the FP64 pipe, at about
+            // 1/60 of the FP32 rate on GB300, otherwise co-limits this pass).
+            for (; i + 15 * 32 < rows; i += 16 * 32) {
                 T s = 0;
 #pragma unroll
-                for (int u = 0; u < 8; ++u) s += q[i + u * 32] * vs[i + u * 32];
+                for (int u = 0; u < 16; ++u) s += q[i + u * 32] * vs[i + u * 32];
                 acc += static_cast<double>(s);
             }
             {
