@@ -270,8 +270,10 @@ def run_batch(args):
                                "extra_work 7, tol 1e-5" % (len(inputs), k),
                    "total_nnz": int(nnz.sum()), "total_cells": int(sizes.sum()),
                    "l2_flush": "inputs larger than L2 (%.1f GB stored)" % (nnz.sum() * 12 / 1e9),
-                   "parallelism": "single GPU, one CTA per matrix"},
+                   "parallelism": "single GPU; cluster teams of 1, 2 or 4 CTAs for the largest matrices, "
+                                  "one CTA per matrix for the rest"},
         "converged": int(conv), "single_matrix_resolves": st["single"], "ctas": st["ctas"],
+        "team_ctas": st.get("team"), "joint_matrices": st.get("joint"),
         "lanczos_steps_total": int(steps.sum()),
         "per_matrix_ms": {"min": float(per_ms.min()), "median": float(np.median(per_ms)),
                           "p90": float(np.percentile(per_ms, 90)), "max": float(per_ms.max()),
