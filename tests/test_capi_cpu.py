@@ -85,3 +85,23 @@ def test_operator_constructors_check_arguments_without_gpu():
     with pytest.raises(eng.IrlbaError) as e:
         eng.DeviceOperatorMatrix(10, 5, lambda adjoint, x, y, stream: None)
     assert e.value.status == eng.ERROR_CUDA
+
+
+def test_dropin_header_and_operator_example_compile(tmp_path):
+    """The header-style drop-in (a user's own Matrix subclass, decorators over it,
+    gpu::DeviceMatrix) and the CUDA residual-operator example build against the
+    engine library without a GPU."""
+    import shutil
+    import subprocess
+    libdir = os.path.dirname(eng.library_path())
+    exe = str(tmp_path / "dropin_test")
+    subprocess.run(["g++", "-std=c++17", "-O0", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "dropin_test.cpp"), "-o", exe, "-L", libdir,
+                    "-lirlba_gb300", "-Wl,-rpath," + libdir], check=True)
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-c",
+                    "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "residual_operator.cu"), "-o", str(tmp_path / "res.o")],
+                   check=True)
