@@ -1,4 +1,5 @@
-"""ORACLE — test infrastructure only (the CPU checker and the timed CPU baseline).
+"""ORACLE — test infrastructure only (the CPU reference results the GPU engine is
+compared with, and the timed CPU baseline).
 
 Python bindings of oracle/irlba_oracle.cpp, a plain-C++ restatement of CppIrlba's
 IRLBA path on column-major arrays. Only tests/, __graft_entry__.smoke() and the

@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only. Nothing in the product path links, loads or
-// calls this file; it is the CPU checker that the GPU engine is compared with, and
-// the CPU baseline that bench.py times beside it.
+// calls this file; it gives the CPU results that the GPU engine is compared with,
+// and the CPU baseline that bench.py times beside it.
 //
 // A plain-C++ restatement of CppIrlba's augmented implicitly restarted Lanczos
 // bidiagonalization (IRLBA) on column-major double arrays. Every function cites
