@@ -145,6 +145,14 @@ class Clocks:
                 "reasons": sorted(reasons)}
 
 
+# DRAM traffic of the SpMV pair per stored nonzero, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the same kernels on the
+# 800,000-cell case of the headline workload (160,011,127 nonzeros; multiply
+# 973.8 MB, adjoint 967.8 MB per launch). The traffic is the stored bytes (FP32
+# value + u16 panel offset) plus vectors, so it scales with the nonzeros.
+SPMV_TRAFFIC_PER_NNZ = {"mul": 973.8e6 / 160011127, "adj": 967.8e6 / 160011127}
+
+
 def spmv_alg_bytes(rows, cols, nnz, vec_bytes, val_bytes=4, idx_bytes=4):
     """Algorithmic bytes of one SpMV on the int32-index basis:
     nnz (val + idx) + (rows + 1) 8-byte pointers + input and output vectors."""
@@ -667,7 +675,16 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "spmv (multiply + adjoint, fused centre/scale)",
                      "achieved": both, "peak": peak, "unit": "GB/s",
                      "frac": (both / peak) if both else None, "peak_source": peak_kind,
-                     "traffic": None,
+                     "traffic": 0.5 * (SPMV_TRAFFIC_PER_NNZ["mul"] + SPMV_TRAFFIC_PER_NNZ["adj"]) * nnz,
+                     "traffic_source": "ncu DRAM bytes per nonzero on the 800,000-cell case, scaled by nonzeros",
+                     "traffic_per_launch": {k: v * nnz for k, v in SPMV_TRAFFIC_PER_NNZ.items()},
+                     # DRAM bandwidth actually drawn (traffic / launch time): the
+                     # int32-index algorithmic basis above counts 8 B per nonzero,
+                     # the stored layout moves about 6.
+                     "traffic_gbs": ((SPMV_TRAFFIC_PER_NNZ["mul"] + SPMV_TRAFFIC_PER_NNZ["adj"]) * nnz /
+                                     ((t_mul + t_adj) * 1e-3) / 1e9) if t_mul + t_adj > 0 else None,
+                     "traffic_frac": ((SPMV_TRAFFIC_PER_NNZ["mul"] + SPMV_TRAFFIC_PER_NNZ["adj"]) * nnz /
+                                      ((t_mul + t_adj) * 1e-3) / 1e9 / peak) if t_mul + t_adj > 0 and peak else None,
                      "achieved_mul": gbs_mul, "achieved_adj": gbs_adj,
                      "alg_bytes_per_launch": {"mul": b_mul, "adj": b_adj},
                      "stored_bytes_per_nnz": {"mul": lay["value_bytes"] + lay["index_bytes_mul"],
