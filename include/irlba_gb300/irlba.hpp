@@ -5,7 +5,7 @@
 //   irlba::Options                      Options.hpp:19-83
 //   irlba::Matrix, Workspace,
 //     AdjointWorkspace, RealizeWorkspace Matrix/interface.hpp:23-223
-//   irlba::SimpleMatrix                 Matrix/simple.hpp:124-178 (dense input)
+//   irlba::SimpleMatrix                 Matrix/simple.hpp:124-178 (dense or Eigen sparse input)
 //   irlba::ParallelSparseMatrix         Matrix/sparse.hpp:438-589
 //   irlba::CenteredMatrix               Matrix/centered.hpp:139-204
 //   irlba::ScaledMatrix                 Matrix/scaled.hpp:195-268
@@ -344,27 +344,94 @@ private:
 
 }  // namespace gpu
 
-// SimpleMatrix over a dense matrix (simple.hpp:124-178). The data are copied
-// to the device at construction.
+namespace gpu {
+
+// Compressed sparse storage in Eigen's layout (Eigen::SparseMatrix and maps of
+// it): valuePtr(), innerIndexPtr() and outerIndexPtr(), column-major unless the
+// type's IsRowMajor is true. In Eigen's uncompressed mode innerNonZeroPtr() is
+// not NULL and gives the entry count of each outer vector.
+template <class T, class = void>
+struct is_compressed_sparse : std::false_type {};
+template <class T>
+struct is_compressed_sparse<T, std::void_t<decltype(std::declval<const T&>().valuePtr()),
+                                           decltype(std::declval<const T&>().innerIndexPtr()),
+                                           decltype(std::declval<const T&>().outerIndexPtr())>> : std::true_type {};
+
+template <class T, class = void>
+struct has_inner_nonzeros : std::false_type {};
+template <class T>
+struct has_inner_nonzeros<T, std::void_t<decltype(std::declval<const T&>().innerNonZeroPtr())>> : std::true_type {};
+
+// The entries of a compressed sparse matrix as the C ABI takes them: int64
+// pointers over the outer dimension (columns, or rows when row-major), int32
+// inner indices and the values, in either storage mode.
+template <class S, class V>
+void compressed_arrays(const S& m, std::vector<int64_t>& ptr, std::vector<int32_t>& idx, std::vector<V>& val) {
+    const Index outer = is_row_major<S>::value ? m.rows() : m.cols();
+    const auto* op = m.outerIndexPtr();
+    const auto* ip = m.innerIndexPtr();
+    const auto* vp = m.valuePtr();
+    const decltype(op) counts = [&]() -> decltype(op) {
+        if constexpr (has_inner_nonzeros<S>::value) return m.innerNonZeroPtr();
+        else return nullptr;
+    }();
+    ptr.assign(static_cast<size_t>(outer) + 1, 0);
+    for (Index o = 0; o < outer; ++o)
+        ptr[o + 1] = ptr[o] + static_cast<int64_t>(counts ? counts[o] : op[o + 1] - op[o]);
+    idx.resize(static_cast<size_t>(ptr[outer]));
+    val.resize(static_cast<size_t>(ptr[outer]));
+    for (Index o = 0; o < outer; ++o) {
+        const int64_t src = static_cast<int64_t>(op[o]);
+        for (int64_t k = 0; k < ptr[o + 1] - ptr[o]; ++k) {
+            idx[ptr[o] + k] = static_cast<int32_t>(ip[src + k]);
+            val[ptr[o] + k] = static_cast<V>(vp[src + k]);
+        }
+    }
+}
+
+}  // namespace gpu
+
+// SimpleMatrix over a dense matrix or an Eigen-style compressed sparse matrix
+// (simple.hpp:124-178 wraps either). The data are copied to the device at
+// construction: dense input as it is, sparse input through the same device
+// layout as ParallelSparseMatrix.
 template <class EigenVector_, class EigenMatrix_, class Simple_>
 class SimpleMatrix final : public gpu::HandleMatrix<EigenVector_, EigenMatrix_> {
 public:
     explicit SimpleMatrix(Simple_ matrix) : my_matrix(std::move(matrix)) {
         const auto& m = gpu::deref(my_matrix);
         typedef typename std::remove_cv<typename std::remove_reference<decltype(m)>::type>::type M;
-        typedef typename std::remove_cv<typename std::remove_pointer<decltype(m.data())>::type>::type Scalar;
         const bool rm = gpu::is_row_major<M>::value;
         irlba_gb300_matrix* h = nullptr;
-        const irlba_gb300_value_type vt = std::is_same<Scalar, float>::value ? IRLBA_GB300_VALUE_F32 : IRLBA_GB300_VALUE_F64;
-        std::vector<double> conv;
-        const void* data = m.data();
-        if (!std::is_same<Scalar, float>::value && !std::is_same<Scalar, double>::value) {
-            conv.assign(m.data(), m.data() + m.rows() * m.cols());
-            data = conv.data();
+        if constexpr (gpu::is_compressed_sparse<M>::value) {
+            typedef typename std::remove_cv<typename std::remove_pointer<decltype(m.valuePtr())>::type>::type Scalar;
+            std::vector<int64_t> ptr;
+            std::vector<int32_t> idx;
+            if (std::is_same<Scalar, float>::value) {
+                std::vector<float> val;
+                gpu::compressed_arrays(m, ptr, idx, val);
+                gpu::check(irlba_gb300_matrix_create_sparse(m.rows(), m.cols(), val.data(), IRLBA_GB300_VALUE_F32,
+                                                            idx.data(), ptr.data(), rm ? 0 : 1, gpu::default_form(), &h));
+            } else {
+                std::vector<double> val;
+                gpu::compressed_arrays(m, ptr, idx, val);
+                gpu::check(irlba_gb300_matrix_create_sparse(m.rows(), m.cols(), val.data(), IRLBA_GB300_VALUE_F64,
+                                                            idx.data(), ptr.data(), rm ? 0 : 1, gpu::default_form(), &h));
+            }
+        } else {
+            typedef typename std::remove_cv<typename std::remove_pointer<decltype(m.data())>::type>::type Scalar;
+            const irlba_gb300_value_type vt =
+                std::is_same<Scalar, float>::value ? IRLBA_GB300_VALUE_F32 : IRLBA_GB300_VALUE_F64;
+            std::vector<double> conv;
+            const void* data = m.data();
+            if (!std::is_same<Scalar, float>::value && !std::is_same<Scalar, double>::value) {
+                conv.assign(m.data(), m.data() + m.rows() * m.cols());
+                data = conv.data();
+            }
+            const int64_t ld = rm ? m.cols() : m.rows();
+            gpu::check(irlba_gb300_matrix_create_dense(m.rows(), m.cols(), data, vt, ld > 0 ? ld : 1, rm ? 1 : 0,
+                                                       gpu::default_form(), &h));
         }
-        const int64_t ld = rm ? m.cols() : m.rows();
-        gpu::check(irlba_gb300_matrix_create_dense(m.rows(), m.cols(), data, vt, ld > 0 ? ld : 1, rm ? 1 : 0,
-                                                   gpu::default_form(), &h));
         this->my_handle = gpu::adopt(h);
         this->my_nrow = m.rows();
         this->my_ncol = m.cols();

@@ -105,3 +105,19 @@ def test_dropin_header_and_operator_example_compile(tmp_path):
                     "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "residual_operator.cu"), "-o", str(tmp_path / "res.o")],
                    check=True)
+
+
+def test_dropin_sparse_input_conversion(tmp_path):
+    """SimpleMatrix / compute_simple / pca accept Eigen-style compressed sparse
+    input (simple.hpp wraps Eigen sparse matrices too; the reference's tests
+    Simple.Sparse, Compute.Sparse and Pca.Sparse use it): the conversion of
+    compressed and uncompressed storage, column- and row-major, FP64 and FP32,
+    into the C ABI's arrays is checked on the host."""
+    import subprocess
+    libdir = os.path.dirname(eng.library_path())
+    exe = str(tmp_path / "sparse_input_test")
+    subprocess.run(["g++", "-std=c++17", "-O0", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "sparse_input_test.cpp"), "-o", exe, "-L", libdir,
+                    "-lirlba_gb300", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([exe], check=True, stdout=subprocess.PIPE, text=True).stdout
+    assert out.strip() == "ok"
