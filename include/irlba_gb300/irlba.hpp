@@ -35,6 +35,27 @@
 
 #include "../irlba_gb300.h"
 
+// Default vector and matrix types of Options, compute(), compute_simple() and
+// pca(), as in the reference (Options.hpp:19, compute.hpp:403,426, pca.hpp:197:
+// Eigen::VectorXd and Eigen::MatrixXd). With Eigen on the include path those are
+// the defaults here too; a caller may instead define both
+// IRLBA_GB300_DEFAULT_VECTOR and IRLBA_GB300_DEFAULT_MATRIX before including
+// this header. Without either, the types must be given explicitly.
+#if !defined(IRLBA_GB300_DEFAULT_VECTOR) && defined(__has_include)
+#if __has_include(<Eigen/Dense>)
+#include <Eigen/Dense>
+#define IRLBA_GB300_DEFAULT_VECTOR Eigen::VectorXd
+#define IRLBA_GB300_DEFAULT_MATRIX Eigen::MatrixXd
+#endif
+#endif
+#if defined(IRLBA_GB300_DEFAULT_VECTOR) && defined(IRLBA_GB300_DEFAULT_MATRIX)
+#define IRLBA_GB300_VECTOR_DEFAULT_ARG = IRLBA_GB300_DEFAULT_VECTOR
+#define IRLBA_GB300_MATRIX_DEFAULT_ARG = IRLBA_GB300_DEFAULT_MATRIX
+#else
+#define IRLBA_GB300_VECTOR_DEFAULT_ARG
+#define IRLBA_GB300_MATRIX_DEFAULT_ARG
+#endif
+
 namespace irlba {
 
 typedef std::ptrdiff_t Index;
@@ -146,7 +167,7 @@ const irlba_gb300_matrix* handle_or_host_operator(const Matrix_& m, std::shared_
 // ---------------------------------------------------------------------------
 // Options (Options.hpp:19-83)
 // ---------------------------------------------------------------------------
-template <class EigenVector_>
+template <class EigenVector_ IRLBA_GB300_VECTOR_DEFAULT_ARG>
 struct Options {
     double invariant_subspace_tolerance = -1;
     double convergence_tolerance = 1e-5;
@@ -604,7 +625,8 @@ struct Results {
     bool converged;
 };
 
-template <class EigenMatrix_, class EigenVector_, class Matrix_>
+template <class EigenMatrix_ IRLBA_GB300_MATRIX_DEFAULT_ARG, class EigenVector_ IRLBA_GB300_VECTOR_DEFAULT_ARG,
+          class Matrix_>
 Results<EigenMatrix_, EigenVector_> compute(const Matrix_& matrix, Index number, const Options<EigenVector_>& options) {
     Results<EigenMatrix_, EigenVector_> output;
     const auto stats = compute(matrix, number, output.U, output.V, output.D, options);
@@ -621,7 +643,8 @@ std::pair<bool, int> compute_simple(const InputEigenMatrix_& matrix, Index numbe
     return compute(wrapped, number, outU, outV, outD, options);
 }
 
-template <class OutputEigenMatrix_, class EigenVector_, class InputEigenMatrix_>
+template <class OutputEigenMatrix_ IRLBA_GB300_MATRIX_DEFAULT_ARG, class EigenVector_ IRLBA_GB300_VECTOR_DEFAULT_ARG,
+          class InputEigenMatrix_>
 Results<OutputEigenMatrix_, EigenVector_> compute_simple(const InputEigenMatrix_& matrix, Index number,
                                                          const Options<EigenVector_>& options) {
     Results<OutputEigenMatrix_, EigenVector_> output;
@@ -672,7 +695,8 @@ std::pair<bool, int> pca(const InputEigenMatrix_& matrix, bool center, bool scal
                               rotation, variances, options);
 }
 
-template <class OutputEigenMatrix_, class EigenVector_, class InputEigenMatrix_>
+template <class OutputEigenMatrix_ IRLBA_GB300_MATRIX_DEFAULT_ARG, class EigenVector_ IRLBA_GB300_VECTOR_DEFAULT_ARG,
+          class InputEigenMatrix_>
 PcaResults<OutputEigenMatrix_, EigenVector_> pca(const InputEigenMatrix_& matrix, bool center, bool scale,
                                                  Index number, const Options<EigenVector_>& options) {
     PcaResults<OutputEigenMatrix_, EigenVector_> output;

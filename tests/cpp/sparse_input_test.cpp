@@ -1,4 +1,5 @@
-// Eigen-style sparse input to the header-style drop-in: the conversion of
+// Eigen-style sparse input to the header-style drop-in, and the reference's
+// default template types (Options, compute, compute_simple, pca): the conversion of
 // compressed and uncompressed storage (column- and row-major) into the C ABI's
 // compressed arrays, checked on the host. SimpleMatrix / compute_simple / pca
 // over a sparse matrix are instantiated too (they need a GPU to run, so the
@@ -7,12 +8,11 @@
 // SparseStore mimics the storage members Eigen documents for
 // Eigen::SparseMatrix (valuePtr, innerIndexPtr, outerIndexPtr, innerNonZeroPtr,
 // IsRowMajor); Eigen itself is not needed.
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
 #include <vector>
-
-#include "irlba_gb300/irlba.hpp"
 
 struct Vec {
     std::vector<double> v;
@@ -32,6 +32,13 @@ struct Mat {
     void resize(std::ptrdiff_t r, std::ptrdiff_t c) { nr = r; nc = c; v.assign(r * c, 0.0); }
     double& operator()(std::ptrdiff_t r, std::ptrdiff_t c) { return v[c * nr + r]; }
 };
+
+// The reference's callers rely on Eigen::VectorXd / Eigen::MatrixXd being the
+// default types of Options, compute(), compute_simple() and pca(); here the
+// stand-in types play that part.
+#define IRLBA_GB300_DEFAULT_VECTOR Vec
+#define IRLBA_GB300_DEFAULT_MATRIX Mat
+#include "irlba_gb300/irlba.hpp"
 
 template <bool RowMajor, typename Scalar>
 struct SparseStore {
@@ -102,13 +109,14 @@ static void check(bool compressed) {
 }
 
 // Instantiated only: needs a GPU to run.
+// Written as the reference's own tests call these (default template types).
 static void run_on_gpu() {
     const auto s = build<false, double>(true);
-    irlba::Options<Vec> opt;
+    irlba::Options opt;
     irlba::SimpleMatrix<Vec, Mat, const SparseStore<false, double>*> wrapped(&s);
-    auto res = irlba::compute<Mat, Vec>(wrapped, 2, opt);
-    auto res2 = irlba::compute_simple<Mat, Vec>(s, 2, opt);
-    auto pcs = irlba::pca<Mat, Vec>(s, true, true, 2, opt);
+    auto res = irlba::compute(wrapped, 2, opt);
+    auto res2 = irlba::compute_simple(s, 2, opt);
+    auto pcs = irlba::pca(s, true, true, 2, opt);
     std::printf("%g %g %g\n", res.D.v[0], res2.D.v[0], pcs.variances.v[0]);
 }
 
