@@ -21,6 +21,7 @@
 #ifndef IRLBA_GB300_IRLBA_HPP
 #define IRLBA_GB300_IRLBA_HPP
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <functional>
@@ -462,8 +463,66 @@ private:
     Simple_ my_matrix;
 };
 
+namespace gpu {
+
+// The host thread partitions ParallelSparseMatrix reports for num_threads > 1
+// (sparse.hpp:53-113; the device uses its own split, so these only keep the
+// accessors' values): each thread gets an equal share of the nonzeros, the
+// first (nnz % num_threads) threads one more. primary[t], primary[t + 1] bound
+// thread t's primary elements (the last element whose cumulative count is
+// within the thread's cumulative share); secondary[t], secondary[t + 1] bound
+// its secondary elements (cumulative per-secondary counts, stepping past the
+// share by at most one element); secondary_nonzero[t][c] is where thread t's
+// secondary range starts within primary element c.
+struct ThreadPartitions {
+    std::vector<Index> primary, secondary;
+    std::vector<std::vector<int64_t>> secondary_nonzero;
+};
+
+inline ThreadPartitions thread_partitions(Index primary_dim, Index secondary_dim, const int64_t* ptr,
+                                          const int32_t* idx, int num_threads) {
+    ThreadPartitions out;
+    if (num_threads <= 1) return out;
+    const int64_t total = ptr[primary_dim];
+    const auto share_end = [&](int t) {  // cumulative nonzeros of threads 0..t
+        const int64_t base = total / num_threads, extra = total % num_threads;
+        return base * (t + 1) + std::min<int64_t>(t + 1, extra);
+    };
+    out.primary.assign(static_cast<size_t>(num_threads) + 1, 0);
+    Index p = 0;
+    for (int t = 0; t < num_threads; ++t) {
+        const int64_t end = share_end(t);
+        while (p < primary_dim && ptr[p + 1] <= end) ++p;
+        out.primary[t + 1] = p;
+    }
+    std::vector<int64_t> per_secondary(static_cast<size_t>(secondary_dim), 0);
+    for (int64_t k = 0; k < total; ++k) ++per_secondary[idx[k]];
+    out.secondary.assign(static_cast<size_t>(num_threads) + 1, 0);
+    Index q = 0;
+    int64_t seen = 0;
+    for (int t = 0; t < num_threads; ++t) {
+        const int64_t end = share_end(t);
+        while (q < secondary_dim && seen <= end) seen += per_secondary[q++];
+        out.secondary[t + 1] = q;
+    }
+    out.secondary_nonzero.assign(static_cast<size_t>(num_threads) + 1,
+                                 std::vector<int64_t>(static_cast<size_t>(primary_dim), 0));
+    for (Index c = 0; c < primary_dim; ++c) {
+        int64_t k = ptr[c];
+        out.secondary_nonzero[0][c] = k;
+        for (int t = 1; t <= num_threads; ++t) {
+            while (k < ptr[c + 1] && idx[k] < out.secondary[t]) ++k;
+            out.secondary_nonzero[t][c] = k;
+        }
+    }
+    return out;
+}
+
+}  // namespace gpu
+
 // ParallelSparseMatrix (sparse.hpp:469): compressed sparse column/row data.
-// num_threads is accepted for interface parity; the device sets its own split.
+// num_threads is accepted for interface parity; the device sets its own split,
+// and the host partitions of the reference are kept for its accessors.
 template <class EigenVector_, class EigenMatrix_, class ValueArray_, class IndexArray_, class PointerArray_>
 class ParallelSparseMatrix final : public gpu::HandleMatrix<EigenVector_, EigenMatrix_> {
 public:
@@ -500,14 +559,32 @@ public:
         this->my_handle = gpu::adopt(h);
         this->my_nrow = nrow;
         this->my_ncol = ncol;
+        if (num_threads > 1) {
+            gpu::ThreadPartitions parts =
+                gpu::thread_partitions(primary, column_major ? nrow : ncol, ptr.data(), idx.data(), num_threads);
+            my_primary_boundaries = std::move(parts.primary);
+            my_secondary_boundaries = std::move(parts.secondary);
+            for (const auto& starts : parts.secondary_nonzero)
+                my_secondary_nonzero_boundaries.emplace_back(starts.begin(), starts.end());
+        }
     }
+    typedef typename std::remove_cv<
+        typename std::remove_reference<decltype(std::declval<const PointerArray_&>()[0])>::type>::type PointerType;
     const ValueArray_& get_values() const { return my_values; }
     const IndexArray_& get_indices() const { return my_indices; }
     const PointerArray_& get_pointers() const { return my_ptrs; }
     bool get_column_major() const { return my_column_major; }
     int get_num_threads() const { return my_num_threads; }
+    // Host thread partitions (sparse.hpp:521-553); set only when num_threads > 1.
+    const std::vector<Index>& get_primary_boundaries() const { return my_primary_boundaries; }
+    const std::vector<Index>& get_secondary_boundaries() const { return my_secondary_boundaries; }
+    const std::vector<std::vector<PointerType>>& get_secondary_nonzero_boundaries() const {
+        return my_secondary_nonzero_boundaries;
+    }
 
 private:
+    std::vector<Index> my_primary_boundaries, my_secondary_boundaries;
+    std::vector<std::vector<PointerType>> my_secondary_nonzero_boundaries;
     ValueArray_ my_values;
     IndexArray_ my_indices;
     PointerArray_ my_ptrs;

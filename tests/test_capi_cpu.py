@@ -121,3 +121,32 @@ def test_dropin_sparse_input_conversion(tmp_path):
                     "-lirlba_gb300", "-Wl,-rpath," + libdir], check=True)
     out = subprocess.run([exe], check=True, stdout=subprocess.PIPE, text=True).stdout
     assert out.strip() == "ok"
+
+
+def test_dropin_thread_partitions_match_oracle(tmp_path):
+    """The drop-in ParallelSparseMatrix reports the reference's host thread
+    partitions (get_primary_boundaries, get_secondary_boundaries,
+    get_secondary_nonzero_boundaries; sparse.hpp:53-113): the header's
+    computation matches the oracle's for several shapes and thread counts."""
+    import json
+    import subprocess
+    import oracle
+    libdir = os.path.dirname(eng.library_path())
+    exe = str(tmp_path / "partitions_test")
+    subprocess.run(["g++", "-std=c++17", "-O0", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "partitions_test.cpp"), "-o", exe, "-L", libdir,
+                    "-lirlba_gb300", "-Wl,-rpath," + libdir], check=True)
+    cases = json.loads(subprocess.run([exe], check=True, stdout=subprocess.PIPE, text=True).stdout)
+    oracle.load()
+    checked = 0
+    for cs in cases:
+        ptr = np.array(cs["ptr"], dtype=np.int64)
+        idx = np.array(cs["idx"], dtype=np.int32)
+        spec = oracle.Spec.sparse(cs["nrow"], cs["ncol"], np.ones(idx.size), idx, ptr, True, 1)
+        for nt, got in cs["parts"].items():
+            pb, sb, snz = oracle.partitions(spec, int(nt))
+            np.testing.assert_array_equal(got["primary"], pb)
+            np.testing.assert_array_equal(got["secondary"], sb)
+            np.testing.assert_array_equal(np.array(got["secondary_nonzero"]).reshape(snz.shape), snz)
+            checked += 1
+    assert checked == 7
