@@ -12,6 +12,7 @@
 //   irlba::compute, compute_simple,
 //     Results                           compute.hpp:141-433
 //   irlba::pca, PcaResults              pca.hpp:55-204
+//   irlba::parallelize, EigenThreadScope parallel.hpp:32-106
 // Vector and matrix types are template parameters as in the reference; they
 // need data(), size() / rows(), cols() and resize(), which Eigen's dense types
 // provide. Matrices are column-major (a type with a static `IsRowMajor` true is
@@ -24,12 +25,14 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdint>
+#include <exception>
 #include <functional>
 #include <memory>
 #include <optional>
 #include <random>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -164,6 +167,75 @@ const irlba_gb300_matrix* handle_or_host_operator(const Matrix_& m, std::shared_
 }
 
 }  // namespace gpu
+
+// ---------------------------------------------------------------------------
+// parallelize and EigenThreadScope (parallel.hpp:32-106), for callers' own
+// Matrix implementations. The engine itself runs on the device and uses
+// neither.
+// ---------------------------------------------------------------------------
+
+// Runs run_task(t) for t in [0, num_tasks), one worker per task, and returns
+// when all have finished; with the IRLBA_CUSTOM_PARALLEL function-like macro
+// defined, that macro is called instead (same arguments). An exception thrown
+// by a task is rethrown here after every worker has joined.
+template <typename Task_, class Run_>
+void parallelize(Task_ num_tasks, Run_ run_task) {
+#ifdef IRLBA_CUSTOM_PARALLEL
+    IRLBA_CUSTOM_PARALLEL(num_tasks, run_task);
+#else
+    if (num_tasks <= 0) return;
+    if (num_tasks == 1) {
+        run_task(static_cast<Task_>(0));
+        return;
+    }
+    std::vector<std::exception_ptr> errors(static_cast<size_t>(num_tasks));
+    std::vector<std::thread> workers;
+    workers.reserve(static_cast<size_t>(num_tasks) - 1);
+    auto guarded_task = [&](Task_ t) {
+        try {
+            run_task(t);
+        } catch (...) {
+            errors[static_cast<size_t>(t)] = std::current_exception();
+        }
+    };
+    for (Task_ t = 1; t < num_tasks; ++t) workers.emplace_back(guarded_task, t);
+    guarded_task(static_cast<Task_>(0));
+    for (auto& w : workers) w.join();
+    for (auto& e : errors)
+        if (e) std::rethrow_exception(e);
+#endif
+}
+
+// Restricts the threads of the caller's Eigen operations while it lives, as the
+// reference does: num_threads when the parallelization scheme is OpenMP
+// (IRLBA_CUSTOM_PARALLEL with IRLBA_CUSTOM_PARALLEL_USES_OPENMP), else 1 (the
+// default parallelize() above uses its own threads). No effect without Eigen or
+// without OpenMP.
+class EigenThreadScope {
+public:
+#if defined(_OPENMP) && defined(EIGEN_WORLD_VERSION)
+    EigenThreadScope(int num_threads) : my_previous(Eigen::nbThreads()) {
+#if defined(IRLBA_CUSTOM_PARALLEL) && defined(IRLBA_CUSTOM_PARALLEL_USES_OPENMP)
+        Eigen::setNbThreads(num_threads);
+#else
+        (void)num_threads;
+        Eigen::setNbThreads(1);
+#endif
+    }
+    ~EigenThreadScope() { Eigen::setNbThreads(my_previous); }
+
+private:
+    int my_previous;
+
+public:
+#else
+    EigenThreadScope(int /*num_threads*/) {}
+#endif
+    EigenThreadScope(const EigenThreadScope&) = delete;
+    EigenThreadScope(EigenThreadScope&&) = delete;
+    EigenThreadScope& operator=(const EigenThreadScope&) = delete;
+    EigenThreadScope& operator=(EigenThreadScope&&) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // Options (Options.hpp:19-83)

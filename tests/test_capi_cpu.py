@@ -150,3 +150,22 @@ def test_dropin_thread_partitions_match_oracle(tmp_path):
             np.testing.assert_array_equal(np.array(got["secondary_nonzero"]).reshape(snz.shape), snz)
             checked += 1
     assert checked == 7
+
+
+@pytest.mark.parametrize("custom", [False, True])
+def test_dropin_parallelize_and_forwarding_header(tmp_path, custom):
+    """irlba::parallelize / EigenThreadScope (parallel.hpp:32-106) through the
+    reference's own header name irlba/irlba.hpp: default workers (all tasks run,
+    a task's exception reaches the caller) and a caller-defined
+    IRLBA_CUSTOM_PARALLEL."""
+    import subprocess
+    libdir = os.path.dirname(eng.library_path())
+    exe = str(tmp_path / "parallel_test")
+    cmd = ["g++", "-std=c++17", "-O0", "-Wall", "-Werror", "-pthread", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cpp", "parallel_test.cpp"), "-o", exe, "-L", libdir, "-lirlba_gb300",
+           "-Wl,-rpath," + libdir]
+    if custom:
+        cmd.insert(1, "-DUSE_CUSTOM_RUNNER")
+    subprocess.run(cmd, check=True)
+    out = subprocess.run([exe], check=True, stdout=subprocess.PIPE, text=True).stdout
+    assert out.strip() == "ok"
