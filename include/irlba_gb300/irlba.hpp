@@ -492,7 +492,7 @@ void compressed_arrays(const S& m, std::vector<int64_t>& ptr, std::vector<int32_
 template <class EigenVector_, class EigenMatrix_, class Simple_>
 class SimpleMatrix final : public gpu::HandleMatrix<EigenVector_, EigenMatrix_> {
 public:
-    explicit SimpleMatrix(Simple_ matrix) : my_matrix(std::move(matrix)) {
+    SimpleMatrix(Simple_ matrix) : my_matrix(std::move(matrix)) {
         const auto& m = gpu::deref(my_matrix);
         typedef typename std::remove_cv<typename std::remove_reference<decltype(m)>::type>::type M;
         const bool rm = gpu::is_row_major<M>::value;
