@@ -188,6 +188,14 @@ def _check(status):
         raise IrlbaError(status, msg)
 
 
+def _is_scipy_sparse(a):
+    try:
+        import scipy.sparse as sp
+    except ImportError:
+        return False
+    return sp.issparse(a)
+
+
 def _dptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
@@ -351,11 +359,42 @@ class ParallelSparseMatrix(Matrix):
                 "index_bytes_adj": ia.value, "panels_mul": pm.value, "panels_adj": pa.value}
 
 
+def compressed_arrays(matrix):
+    """(values, indices, pointers, column_major) of a scipy.sparse matrix in the
+    C ABI's layout: CSC stays column-major and CSR row-major (any other sparse
+    format is read as CSR); duplicate entries are summed and indices sorted
+    within each row or column, as Eigen's compressed storage has them."""
+    import scipy.sparse as sp
+    if not sp.issparse(matrix):
+        raise TypeError("not a scipy.sparse matrix")
+    column_major = matrix.format == "csc"
+    m = matrix.tocsc() if column_major else matrix.tocsr()
+    m = m.copy()
+    m.sum_duplicates()
+    m.sort_indices()
+    values = np.ascontiguousarray(m.data)
+    if values.dtype not in (np.float32, np.float64):
+        values = values.astype(np.float64)
+    return (values, np.ascontiguousarray(m.indices, dtype=np.int32), np.ascontiguousarray(m.indptr, dtype=np.int64),
+            column_major)
+
+
 class SimpleMatrix(Matrix):
-    """irlba::SimpleMatrix over a dense matrix (Matrix/simple.hpp:124-178)."""
+    """irlba::SimpleMatrix over a dense matrix or a sparse one
+    (Matrix/simple.hpp:124-178 wraps either Eigen type); scipy.sparse input is
+    stored in the same device layout as ParallelSparseMatrix."""
 
     def __init__(self, dense, form=FORM_FP64):
         lib = load_library()
+        if _is_scipy_sparse(dense):
+            x, i, p, column_major = compressed_arrays(dense)
+            nrow, ncol = dense.shape
+            h = ctypes.c_void_p()
+            vt = VALUE_F64 if x.dtype == np.float64 else VALUE_F32
+            _check(lib.irlba_gb300_matrix_create_sparse(nrow, ncol, _vptr(x), vt, _vptr(i), _vptr(p),
+                                                        int(column_major), form, ctypes.byref(h)))
+            super().__init__(h.value, nrow, ncol, form)
+            return
         a = np.asarray(dense)
         if a.dtype not in (np.float32, np.float64):
             a = a.astype(np.float64)
@@ -497,9 +536,9 @@ def pca(matrix, center, scale, number, options=None):
     """irlba::pca(matrix, center, scale, number, options) (pca.hpp:197-204).
 
     `matrix` is an undecorated ParallelSparseMatrix or SimpleMatrix (rows are
-    observations, columns are features), or a numpy array (wrapped in a
-    SimpleMatrix)."""
-    if isinstance(matrix, np.ndarray):
+    observations, columns are features), or a numpy array or scipy.sparse
+    matrix (wrapped in a SimpleMatrix)."""
+    if isinstance(matrix, np.ndarray) or _is_scipy_sparse(matrix):
         matrix = SimpleMatrix(matrix)
     options = options or Options()
     keep = []

@@ -169,3 +169,34 @@ def test_dropin_parallelize_and_forwarding_header(tmp_path, custom):
     subprocess.run(cmd, check=True)
     out = subprocess.run([exe], check=True, stdout=subprocess.PIPE, text=True).stdout
     assert out.strip() == "ok"
+
+
+def test_python_sparse_input_arrays():
+    """SimpleMatrix / compute_simple / pca take scipy.sparse input (the Python
+    counterpart of an Eigen sparse matrix): CSC stays column-major, other
+    formats become CSR, duplicates are summed and indices sorted."""
+    sp = pytest.importorskip("scipy.sparse")
+    rng = np.random.default_rng(4)
+    dense = np.where(rng.random((30, 17)) < 0.2, rng.standard_normal((30, 17)), 0.0)
+    rows, cols = np.nonzero(dense)
+    # unsorted COO with a duplicate split of one entry
+    order = rng.permutation(rows.size)
+    r = np.concatenate([rows[order], rows[:1]])
+    c = np.concatenate([cols[order], cols[:1]])
+    v = np.concatenate([dense[rows[order], cols[order]], [0.5]])
+    v[np.where(order == 0)[0][0]] -= 0.5
+    coo = sp.coo_matrix((v, (r, c)), shape=dense.shape)
+    for mat, want_cm in ((sp.csc_matrix(dense), True), (sp.csr_matrix(dense), False), (coo, False),
+                         (sp.csr_matrix(dense, dtype=np.float32), False)):
+        x, i, p, cm = eng.compressed_arrays(mat)
+        assert cm == want_cm and i.dtype == np.int32 and p.dtype == np.int64
+        assert x.dtype in (np.float32, np.float64)
+        back = (sp.csc_matrix if cm else sp.csr_matrix)((x, i, p), shape=dense.shape).toarray()
+        np.testing.assert_allclose(back, dense, rtol=1e-6 if x.dtype == np.float32 else 1e-15, atol=1e-15)
+        for k in range(p.size - 1):
+            assert np.all(np.diff(i[p[k]:p[k + 1]]) > 0)
+    if eng.device_count() > 0:
+        return
+    with pytest.raises(eng.IrlbaError) as e:
+        eng.SimpleMatrix(sp.csr_matrix(dense))
+    assert e.value.status == eng.ERROR_CUDA
