@@ -147,6 +147,8 @@ def load_library():
                                          ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(Stats), P]),
         "irlba_gb300_orthogonalize_vector_device": (i32, [P, i64, i64, i64, P, P]),
         "irlba_gb300_spmv_device": (i32, [P, i32, P, P, P]),
+        "irlba_gb300_matrix_set_vector": (i32, [P, pd]),
+        "irlba_gb300_update_k_device": (i32, [P, i64, P]),
         "irlba_gb300_matrix_layout": (i32, [P, ctypes.POINTER(i64), ctypes.POINTER(i32), ctypes.POINTER(i32),
                                             ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]),
         "irlba_gb300_set_profiling": (None, [i32]),
@@ -563,6 +565,16 @@ def pca(matrix, center, scale, number, options=None):
                       iterations=iters.value, converged=bool(conv.value),
                       center=c_out[:n].copy() if center else None, scale=s_out[:n].copy() if scale else None,
                       stats=_stats_dict(st))
+
+
+def update_k_device(quads):
+    """The device restart step's update_k (compute.hpp:78-111) for an (n, 4)
+    array of (k, requested, n_converged, work); returns the n next k values."""
+    q = np.ascontiguousarray(np.asarray(quads, dtype=np.int32).reshape(-1, 4))
+    out = np.zeros(q.shape[0], dtype=np.int32)
+    _check(load_library().irlba_gb300_update_k_device(ctypes.c_void_p(q.ctypes.data), q.shape[0],
+                                                      ctypes.c_void_p(out.ctypes.data)))
+    return out
 
 
 def device_count():

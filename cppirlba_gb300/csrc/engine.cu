@@ -1691,11 +1691,12 @@ static double* noalloc_scratch_for_current_device() {
 
 // Same operation as irlba_gb300_orthogonalize_vector_device, with no device
 // allocation. The first call on each device looks up the scratch array's
-// device address (make that first call before any stream capture). Calls share
-// the array: calls that overlap on the GPU (other streams, other host threads)
-// race on it. Sizes beyond the scratch are rejected: it needs
-// 128 + round_up(ncols, 32) + max(ceil(L / 1024) * ncols, min(ceil(L / 256), 1216))
-// doubles out of 131072 (1 MiB), e.g. ncols = 64 allows L up to about 2 million.
+// device address (make that first call before any stream capture). The call
+// synchronizes `stream` before it returns. Calls share the array: calls that
+// overlap on the GPU (other streams, other host threads) race on it. Sizes
+// beyond the scratch are rejected: it needs
+// 128 + round_up(max(ncols, 1), 32) + min(ceil(L / 256), 1216) * max(ncols, 1)
+// doubles out of 131072 (1 MiB), so any L is accepted for ncols <= 107.
 irlba_gb300_status irlba_gb300_orthogonalize_vector_device_noalloc(const double* Q, int64_t L, int64_t ldq,
                                                                    int64_t ncols, double* vec, void* stream) {
     return guarded([&]() {
@@ -1726,6 +1727,33 @@ irlba_gb300_status irlba_gb300_orthogonalize_vector_device_noalloc(const double*
     });
 }
 
+// The restart kernel's update_k (compute.hpp:78-111) on the device, for
+// `count` quadruples (k, requested, n_converged, work) in host memory.
+irlba_gb300_status irlba_gb300_update_k_device(const int32_t* args, int64_t count, int32_t* out) {
+    return guarded([&]() {
+        if (count < 0 || (count > 0 && (!args || !out))) invalid("NULL argument");
+        if (count == 0) return;
+        DevBuf da(sizeof(int32_t) * 4 * count), dout(sizeof(int32_t) * count);
+        CUDA_TRY(cudaMemcpy(da.ptr, args, sizeof(int32_t) * 4 * count, cudaMemcpyHostToDevice));
+        launch_update_k(da.as<int32_t>(), count, dout.as<int32_t>(), nullptr);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpy(out, dout.ptr, sizeof(int32_t) * count, cudaMemcpyDeviceToHost));
+    });
+}
+
+// Replaces the centre (CenteredMatrix) or scale (ScaledMatrix) vector of a
+// decorator handle, same length as at creation. The reference's decorators
+// read the caller's vector through a pointer at every product
+// (centered.hpp:139-160, scaled.hpp:195-223); callers that keep that pointer
+// semantics pass the vector's current contents here before a compute call.
+irlba_gb300_status irlba_gb300_matrix_set_vector(irlba_gb300_matrix* matrix, const double* values) {
+    return guarded([&]() {
+        if (!matrix || !values) invalid("NULL argument");
+        if (matrix->kind != 1 && matrix->kind != 2) invalid("set_vector takes a centred or scaled matrix");
+        std::copy(values, values + matrix->vec.size(), matrix->vec.begin());
+    });
+}
+
 // Per-kernel-class timing of the last compute call (ms) when profiling is on.
 // Classes: 0 SpMV multiply, 1 SpMV adjoint, 2 reorthogonalization,
 // 3 restart (small SVD), 4 rotation, 5 other. launches may be NULL.
@@ -1753,23 +1781,31 @@ irlba_gb300_status irlba_gb300_spmv_device(const irlba_gb300_matrix* matrix, int
         const BaseMatrix& A = *matrix->base;
         const DirPlan& p = adjoint ? A.adj : A.mul;
         cudaStream_t s = static_cast<cudaStream_t>(stream);
-        static thread_local DevBuf zero_flag, partial;
-        if (!zero_flag.ptr) {
-            zero_flag.alloc(sizeof(int32_t));
-            CUDA_TRY(cudaMemset(zero_flag.ptr, 0, sizeof(int32_t)));
+        // The abort flag (zero) and the panel partials live in one stream-ordered
+        // allocation on the caller's stream, so calls on different devices or
+        // streams never share scratch.
+        const size_t vbytes = A.form == IRLBA_GB300_FORM_FP64 ? 8 : 4;
+        const size_t pbytes = p.dev.npanels > 1 ? vbytes * static_cast<size_t>(p.dev.npanels * p.dev.nrows) : 0;
+        void* scratch = nullptr;
+        CUDA_TRY(cudaMallocAsync(&scratch, 256 + pbytes, s));
+        int32_t* zero_flag = static_cast<int32_t*>(scratch);
+        void* partial = static_cast<char*>(scratch) + 256;
+        cudaError_t err = cudaMemsetAsync(zero_flag, 0, sizeof(int32_t), s);
+        if (err == cudaSuccess) {
+            if (A.form == IRLBA_GB300_FORM_FP64) {
+                Epilogue<double> e;
+                launch_spmv<double>(p.dev, static_cast<const double*>(x), static_cast<double*>(y),
+                                    static_cast<double*>(partial), e, zero_flag, s);
+            } else {
+                Epilogue<float> e;
+                launch_spmv<float>(p.dev, static_cast<const float*>(x), static_cast<float*>(y),
+                                   static_cast<float*>(partial), e, zero_flag, s);
+            }
+            err = cudaGetLastError();
         }
-        const size_t pbytes = (A.form == IRLBA_GB300_FORM_FP64 ? 8 : 4) * std::max<int64_t>(p.dev.npanels * p.dev.nrows, 1);
-        if (partial.bytes < pbytes) partial.alloc(pbytes);
-        if (A.form == IRLBA_GB300_FORM_FP64) {
-            Epilogue<double> e;
-            launch_spmv<double>(p.dev, static_cast<const double*>(x), static_cast<double*>(y), partial.as<double>(), e,
-                                zero_flag.as<int32_t>(), s);
-        } else {
-            Epilogue<float> e;
-            launch_spmv<float>(p.dev, static_cast<const float*>(x), static_cast<float*>(y), partial.as<float>(), e,
-                               zero_flag.as<int32_t>(), s);
-        }
-        CUDA_TRY(cudaGetLastError());
+        const cudaError_t ferr = cudaFreeAsync(scratch, s);
+        CUDA_TRY(err);
+        CUDA_TRY(ferr);
     });
 }
 

@@ -150,6 +150,9 @@ struct RestartArgs {
     Ctrl* ctrl;
 };
 void launch_restart(const RestartArgs& a, cudaStream_t stream, size_t max_smem);
+// out[i] = the restart kernel's update_k(args[4i], args[4i+1], args[4i+2], args[4i+3])
+// (k, requested, n_converged, work), compute.hpp:78-111.
+void launch_update_k(const int32_t* args, int64_t count, int32_t* out, cudaStream_t stream);
 size_t restart_smem_bytes(int work);
 cudaError_t restart_configure(size_t max_smem);
 

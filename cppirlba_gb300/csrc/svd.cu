@@ -279,6 +279,22 @@ __global__ void __launch_bounds__(kSvdThreads) dense_svd_kernel(const double* A,
 
 }  // namespace
 
+// update_k of the restart kernel evaluated for `count` argument quadruples
+// (k, requested, n_converged, work), so that the device arithmetic can be
+// checked against the reference's known answers.
+static __global__ void update_k_kernel(const int32_t* args, int64_t count, int32_t* out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = jacobi::update_k_dev(args[4 * i], args[4 * i + 1], args[4 * i + 2], args[4 * i + 3]);
+}
+
+void launch_update_k(const int32_t* args, int64_t count, int32_t* out, cudaStream_t stream) {
+    if (count <= 0) return;
+    const int64_t blocks = std::min<int64_t>((count + 255) / 256, 1024);
+    update_k_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(args, count, out);
+    count_launch();
+}
+
 size_t restart_smem_bytes(int work) { return 2 * sizeof(double) * static_cast<size_t>(work) * work; }
 
 // Dynamic shared memory available to the restart kernel: the per-block opt-in

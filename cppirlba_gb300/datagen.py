@@ -33,14 +33,8 @@ GENE_MEAN_SIGMA = 1.5
 DISPERSION = 0.5
 
 
-def _load():
-    global _lib
-    if _lib is not None:
-        return _lib
-    if not os.path.exists(_LIB_PATH):
-        from . import build as _build
-        _build.build()
-    lib = ctypes.CDLL(_LIB_PATH)
+def _declare(lib):
+    """Declares the generator's C entry points on a loaded library."""
     i64, dbl, u64, P = ctypes.c_int64, ctypes.c_double, ctypes.c_uint64, ctypes.c_void_p
     lib.irlba_gb300_datagen_counts.restype = i64
     lib.irlba_gb300_datagen_counts.argtypes = [i64, i64, dbl, u64, ctypes.c_int, P]
@@ -50,17 +44,29 @@ def _load():
     lib.irlba_gb300_datagen_gene_means.argtypes = [i64, dbl, dbl, u64, P]
     lib.irlba_gb300_transpose_compressed.restype = None
     lib.irlba_gb300_transpose_compressed.argtypes = [i64, i64, P, P, P, ctypes.c_int, P, P, P]
-    _lib = lib
     return lib
+
+
+def _load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        from . import build as _build
+        _build.build()
+    _lib = _declare(ctypes.CDLL(_LIB_PATH))
+    return _lib
 
 
 def _p(a):
     return ctypes.c_void_p(a.ctypes.data)
 
 
-def scrna_gene_major(genes, cells, density, seed, dtype=np.float32, threads=None):
-    """Gene-major compressed matrix (genes x cells): (ptr int64, idx int32 cell, values)."""
-    lib = _load()
+def scrna_gene_major(genes, cells, density, seed, dtype=np.float32, threads=None, lib=None):
+    """Gene-major compressed matrix (genes x cells): (ptr int64, idx int32 cell, values).
+    lib: another loaded library that exports the same generator (default: this
+    package's generator library)."""
+    lib = _declare(lib) if lib is not None else _load()
     threads = threads or os.cpu_count() or 1
     ptr = np.zeros(genes + 1, dtype=np.int64)
     nnz = lib.irlba_gb300_datagen_counts(genes, cells, density, seed, threads, _p(ptr))
@@ -71,9 +77,9 @@ def scrna_gene_major(genes, cells, density, seed, dtype=np.float32, threads=None
     return ptr, idx, val
 
 
-def transpose_compressed(primary, secondary, ptr, idx, val):
+def transpose_compressed(primary, secondary, ptr, idx, val, lib=None):
     """(secondary x primary) compressed transpose, indices sorted."""
-    lib = _load()
+    lib = _declare(lib) if lib is not None else _load()
     tptr = np.zeros(secondary + 1, dtype=np.int64)
     tidx = np.empty(idx.shape[0], dtype=np.int32)
     tval = np.empty(val.shape[0], dtype=val.dtype)
@@ -107,12 +113,12 @@ class SparseInput:
         return out
 
 
-def scrna_pca_input(genes, cells, density, seed, dtype, cell_major):
+def scrna_pca_input(genes, cells, density, seed, dtype, cell_major, lib=None):
     """Cells x genes PCA input. cell_major=True gives CSR cells x genes (the
     genes x cells CSC layout); False gives CSC cells x genes (genes x cells CSR)."""
-    ptr, idx, val = scrna_gene_major(genes, cells, density, seed, dtype=dtype)
+    ptr, idx, val = scrna_gene_major(genes, cells, density, seed, dtype=dtype, lib=lib)
     if cell_major:
-        tptr, tidx, tval = transpose_compressed(genes, cells, ptr, idx, val)
+        tptr, tidx, tval = transpose_compressed(genes, cells, ptr, idx, val, lib=lib)
         return SparseInput(cells, genes, tptr, tidx, tval, column_major=False)
     return SparseInput(cells, genes, ptr, idx, val, column_major=True)
 

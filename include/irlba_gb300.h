@@ -207,9 +207,11 @@ irlba_gb300_status irlba_gb300_orthogonalize_vector_device(const double* Q, int6
  * would synchronize the device). No counterpart in the reference. Scratch is a
  * fixed 1 MiB device array per GPU, held until the process exits; the first
  * call on a device looks up its address (make it before any stream capture).
- * Calls that overlap on the GPU race on the shared scratch. Needs
- * 128 + round_up(ncols, 32) + min(ceil(L / 256), 1216) * max(ncols, 1)
- * <= 131072 doubles; larger requests return IRLBA_GB300_ERROR_INVALID_ARGUMENT. */
+ * The call synchronizes `stream` before it returns. Calls that overlap on the
+ * GPU race on the shared scratch. Needs
+ * 128 + round_up(max(ncols, 1), 32) + min(ceil(L / 256), 1216) * max(ncols, 1)
+ * <= 131072 doubles (any L for ncols <= 107); larger requests return
+ * IRLBA_GB300_ERROR_INVALID_ARGUMENT. */
 irlba_gb300_status irlba_gb300_orthogonalize_vector_device_noalloc(const double* Q, int64_t L, int64_t ldq,
                                                                    int64_t ncols, double* vec, void* stream);
 
@@ -237,6 +239,19 @@ irlba_gb300_status irlba_gb300_pca_device(const irlba_gb300_matrix* matrix, int3
  * matrices and FP32 for the FP32 form. Asynchronous on `stream`. */
 irlba_gb300_status irlba_gb300_spmv_device(const irlba_gb300_matrix* matrix, int32_t adjoint, const void* x,
                                            void* y, void* stream);
+
+/* Replaces the centre vector of a CenteredMatrix handle or the scale vector of
+ * a ScaledMatrix handle (same length as at creation). Replaces the pointer
+ * semantics of the reference's decorators, which read the caller's vector at
+ * every product (centered.hpp:139-160, scaled.hpp:195-223). */
+irlba_gb300_status irlba_gb300_matrix_set_vector(irlba_gb300_matrix* matrix, const double* values);
+
+/* update_k of the device restart step (compute.hpp:78-111, irlba::update_k)
+ * evaluated on the GPU for `count` argument quadruples args[4i..4i+3] =
+ * (k, requested, n_converged, work); out[i] receives the next k. Host arrays.
+ * Exposed so the device arithmetic can be checked against the reference's
+ * known answers (tests/src/compute.cpp:52-76). */
+irlba_gb300_status irlba_gb300_update_k_device(const int32_t* args, int64_t count, int32_t* out);
 
 /* Stored layout of an undecorated matrix, for byte accounting. */
 irlba_gb300_status irlba_gb300_matrix_layout(const irlba_gb300_matrix* matrix, int64_t* nnz, int32_t* value_bytes,

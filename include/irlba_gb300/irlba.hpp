@@ -95,6 +95,14 @@ struct is_row_major<T, std::void_t<decltype(T::IsRowMajor)>> : std::integral_con
 template <class P>
 auto& deref(const P& p) { return *p; }
 
+// Dense types with explicit strides (Eigen's Map<..., OuterStride<>>, Block,
+// Ref): the storage of column (or row) j starts at data() + j * outerStride().
+template <class T, class = void>
+struct has_strides : std::false_type {};
+template <class T>
+struct has_strides<T, std::void_t<decltype(std::declval<const T&>().outerStride()),
+                                  decltype(std::declval<const T&>().innerStride())>> : std::true_type {};
+
 // Engine handle of a matrix, or NULL for one the engine cannot run directly
 // (a user's own Matrix subclass, or a type without gpu_handle()).
 template <class M, class = void>
@@ -153,6 +161,23 @@ private:
 
 // Engine handle of `m`: its own, or a host operator over its workspaces (kept
 // alive by `products` and `op`).
+// Passes a decorator's centre or scale vector to the engine again when its
+// contents differ from `seen` (the contents passed last).
+template <class Vector_>
+void refresh_vector(irlba_gb300_matrix* h, const Vector_& v, std::vector<double>& seen) {
+    if (static_cast<size_t>(v.size()) != seen.size()) throw std::runtime_error("decorator vector changed length");
+    const auto* d = v.data();
+    bool same = true;
+    for (size_t i = 0; i < seen.size(); ++i)
+        if (static_cast<double>(d[i]) != seen[i]) {
+            same = false;
+            break;
+        }
+    if (same) return;
+    for (size_t i = 0; i < seen.size(); ++i) seen[i] = static_cast<double>(d[i]);
+    check(irlba_gb300_matrix_set_vector(h, seen.data()));
+}
+
 template <class EigenVector_, class Matrix_>
 const irlba_gb300_matrix* handle_or_host_operator(const Matrix_& m, std::shared_ptr<void>& products, Handle& op) {
     const irlba_gb300_matrix* h = handle_of(m);
@@ -388,15 +413,15 @@ public:
     Index rows() const { return my_nrow; }
     Index cols() const { return my_ncol; }
     std::unique_ptr<Workspace<EigenVector_>> new_workspace() const {
-        return std::make_unique<HandleWorkspace<EigenVector_>>(my_handle.get());
+        return std::make_unique<HandleWorkspace<EigenVector_>>(this->gpu_handle());
     }
     std::unique_ptr<AdjointWorkspace<EigenVector_>> new_adjoint_workspace() const {
-        return std::make_unique<HandleAdjointWorkspace<EigenVector_>>(my_handle.get());
+        return std::make_unique<HandleAdjointWorkspace<EigenVector_>>(this->gpu_handle());
     }
     std::unique_ptr<RealizeWorkspace<EigenMatrix_>> new_realize_workspace() const {
-        return std::make_unique<HandleRealizeWorkspace<EigenMatrix_>>(my_handle.get());
+        return std::make_unique<HandleRealizeWorkspace<EigenMatrix_>>(this->gpu_handle());
     }
-    const irlba_gb300_matrix* gpu_handle() const { return my_handle.get(); }
+    const irlba_gb300_matrix* gpu_handle() const override { return my_handle.get(); }
 
 protected:
     Handle my_handle;
@@ -518,13 +543,30 @@ public:
                 std::is_same<Scalar, float>::value ? IRLBA_GB300_VALUE_F32 : IRLBA_GB300_VALUE_F64;
             std::vector<double> conv;
             const void* data = m.data();
-            if (!std::is_same<Scalar, float>::value && !std::is_same<Scalar, double>::value) {
-                conv.assign(m.data(), m.data() + m.rows() * m.cols());
-                data = conv.data();
+            int64_t ld = rm ? m.cols() : m.rows();
+            bool unit_inner = true;
+            if constexpr (gpu::has_strides<M>::value) {
+                // Strided storage (a Map with an outer stride, a Block): the
+                // engine reads it with the type's own leading dimension.
+                ld = static_cast<int64_t>(m.outerStride());
+                unit_inner = m.innerStride() == 1;
             }
-            const int64_t ld = rm ? m.cols() : m.rows();
-            gpu::check(irlba_gb300_matrix_create_dense(m.rows(), m.cols(), data, vt, ld > 0 ? ld : 1, rm ? 1 : 0,
-                                                       gpu::default_form(), &h));
+            const bool convert = !std::is_same<Scalar, float>::value && !std::is_same<Scalar, double>::value;
+            bool row_major = rm;
+            if (convert || !unit_inner) {
+                // Other scalar types, or a non-unit inner stride: copy to a
+                // contiguous column-major FP64 array.
+                conv.resize(static_cast<size_t>(m.rows() * m.cols()));
+                for (Index c = 0; c < m.cols(); ++c)
+                    for (Index r = 0; r < m.rows(); ++r)
+                        conv[static_cast<size_t>(c * m.rows() + r)] = static_cast<double>(m(r, c));
+                data = conv.data();
+                ld = m.rows();
+                row_major = false;
+            }
+            gpu::check(irlba_gb300_matrix_create_dense(m.rows(), m.cols(), data,
+                                                       (convert || !unit_inner) ? IRLBA_GB300_VALUE_F64 : vt,
+                                                       ld > 0 ? ld : 1, row_major ? 1 : 0, gpu::default_form(), &h));
         }
         this->my_handle = gpu::adopt(h);
         this->my_nrow = m.rows();
@@ -673,10 +715,10 @@ public:
         const auto& inner = gpu::deref(my_matrix);
         const irlba_gb300_matrix* ih = gpu::handle_or_host_operator<EigenVector_>(inner, my_products, my_inner_op);
         const auto& c = gpu::deref(my_center);
-        std::vector<double> cv(c.data(), c.data() + c.size());
-        if (static_cast<Index>(cv.size()) != inner.cols()) throw std::runtime_error("center has the wrong length");
+        my_seen.assign(c.data(), c.data() + c.size());
+        if (static_cast<Index>(my_seen.size()) != inner.cols()) throw std::runtime_error("center has the wrong length");
         irlba_gb300_matrix* h = nullptr;
-        gpu::check(irlba_gb300_matrix_center(ih, cv.data(), &h));
+        gpu::check(irlba_gb300_matrix_center(ih, my_seen.data(), &h));
         this->my_handle = gpu::adopt(h);
         this->my_nrow = inner.rows();
         this->my_ncol = inner.cols();
@@ -684,9 +726,20 @@ public:
 
     ~CenteredMatrix() { this->my_handle.reset(); }
 
+    // Like the reference's decorator, which reads the caller's centre vector
+    // through its pointer at every product (centered.hpp:46-52,83-87), the
+    // engine handle picks up the vector's current contents whenever it is
+    // used (every compute/pca call and every workspace).
+    const irlba_gb300_matrix* gpu_handle() const override {
+        gpu::handle_of(gpu::deref(my_matrix));  // refreshes decorators nested inside
+        gpu::refresh_vector(this->my_handle.get(), gpu::deref(my_center), my_seen);
+        return this->my_handle.get();
+    }
+
 private:
     MatrixPointer_ my_matrix;
     CenterPointer_ my_center;
+    mutable std::vector<double> my_seen;  // the contents last passed to the engine
     std::shared_ptr<void> my_products;  // host products of an inner matrix without an engine handle
     gpu::Handle my_inner_op;
 };
@@ -701,11 +754,11 @@ public:
         const auto& inner = gpu::deref(my_matrix);
         const irlba_gb300_matrix* ih = gpu::handle_or_host_operator<EigenVector_>(inner, my_products, my_inner_op);
         const auto& s = gpu::deref(my_scale);
-        std::vector<double> sv(s.data(), s.data() + s.size());
-        if (static_cast<Index>(sv.size()) != (column ? inner.cols() : inner.rows()))
+        my_seen.assign(s.data(), s.data() + s.size());
+        if (static_cast<Index>(my_seen.size()) != (column ? inner.cols() : inner.rows()))
             throw std::runtime_error("scale has the wrong length");
         irlba_gb300_matrix* h = nullptr;
-        gpu::check(irlba_gb300_matrix_scale(ih, sv.data(), column ? 1 : 0, divide ? 1 : 0, &h));
+        gpu::check(irlba_gb300_matrix_scale(ih, my_seen.data(), column ? 1 : 0, divide ? 1 : 0, &h));
         this->my_handle = gpu::adopt(h);
         this->my_nrow = inner.rows();
         this->my_ncol = inner.cols();
@@ -713,9 +766,18 @@ public:
 
     ~ScaledMatrix() { this->my_handle.reset(); }
 
+    // The scale vector is read at every use, as the reference's decorator
+    // reads it through its pointer (scaled.hpp:52-69,106-123).
+    const irlba_gb300_matrix* gpu_handle() const override {
+        gpu::handle_of(gpu::deref(my_matrix));  // refreshes decorators nested inside
+        gpu::refresh_vector(this->my_handle.get(), gpu::deref(my_scale), my_seen);
+        return this->my_handle.get();
+    }
+
 private:
     MatrixPointer_ my_matrix;
     ScalePointer_ my_scale;
+    mutable std::vector<double> my_seen;  // the contents last passed to the engine
     std::shared_ptr<void> my_products;  // host products of an inner matrix without an engine handle
     gpu::Handle my_inner_op;
 };

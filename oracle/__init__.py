@@ -49,6 +49,7 @@ class OracleMatrixSpec(ctypes.Structure):
         ("scale", ctypes.POINTER(ctypes.c_double)),
         ("scale_column", ctypes.c_int32),
         ("scale_divide", ctypes.c_int32),
+        ("values32", ctypes.POINTER(ctypes.c_float)),
     ]
 
 
@@ -122,7 +123,9 @@ class Spec:
     @staticmethod
     def sparse(nrow, ncol, x, i, p, column_major, num_threads=1, center=None, scale=None, scale_column=True,
                scale_divide=True, center_outer=False):
-        x = np.ascontiguousarray(x, dtype=np.float64)
+        # FP32 values stay FP32 (as a float ValueArray of the reference's
+        # ParallelSparseMatrix); products promote them to FP64.
+        x = np.ascontiguousarray(x, dtype=np.float32 if np.asarray(x).dtype == np.float32 else np.float64)
         i = np.ascontiguousarray(i, dtype=np.int32)
         p = np.ascontiguousarray(p, dtype=np.int64)
         s = OracleMatrixSpec()
@@ -130,7 +133,10 @@ class Spec:
         s.column_major = int(bool(column_major))
         s.num_threads = num_threads
         s.nrow, s.ncol = nrow, ncol
-        s.values = _pd(x)
+        if x.dtype == np.float32:
+            s.values32 = x.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        else:
+            s.values = _pd(x)
         s.indices = i.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
         s.pointers = p.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
         keep = [x, i, p]
@@ -283,6 +289,14 @@ def svd(A):
     V = np.zeros((p, n))
     load().oracle_svd(m, n, _pd(A), _pd(U), _pd(S), _pd(V))
     return U.T.copy(), S, V.T.copy()
+
+
+def scrna_pca_input(genes, cells, density, seed, dtype, cell_major):
+    """The seeded single-cell-like PCA input of cppirlba_gb300.datagen, generated
+    by the same generator source compiled into the oracle library (so that the
+    CPU reference run loads no library of the product)."""
+    from cppirlba_gb300 import datagen
+    return datagen.scrna_pca_input(genes, cells, density, seed, dtype, cell_major, lib=load())
 
 
 def random_normals(n, seed):

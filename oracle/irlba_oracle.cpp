@@ -133,7 +133,8 @@ struct DenseMatrix : public Matrix {
 struct SparseMatrix : public Matrix {
     Index primary_dim, secondary_dim;
     int num_threads;
-    const double* values;
+    const double* values;      // FP64 values, or
+    const float* values32;     // FP32 values (the reference's ValueArray may hold float)
     const int32_t* indices;
     const int64_t* ptrs;
     bool column_major;
@@ -141,9 +142,10 @@ struct SparseMatrix : public Matrix {
     std::vector<std::vector<int64_t>> secondary_nonzero_boundaries;
 
     // ParallelSparseMatrixCore constructor, sparse.hpp:35-115.
-    SparseMatrix(Index nrow, Index ncol, const double* x, const int32_t* i, const int64_t* p, bool cm, int nt)
+    SparseMatrix(Index nrow, Index ncol, const double* x, const int32_t* i, const int64_t* p, bool cm, int nt,
+                 const float* x32 = nullptr)
         : primary_dim(cm ? ncol : nrow), secondary_dim(cm ? nrow : ncol), num_threads(nt),
-          values(x), indices(i), ptrs(p), column_major(cm) {
+          values(x), values32(x32), indices(i), ptrs(p), column_major(cm) {
         if (num_threads > 1) {
             const int64_t total = ptrs[primary_dim];
             const int64_t per_thread_floor = total / num_threads;
@@ -196,13 +198,25 @@ struct SparseMatrix : public Matrix {
     Index rows() const override { return column_major ? secondary_dim : primary_dim; }
     Index cols() const override { return column_major ? primary_dim : secondary_dim; }
 
+    // Calls f with the stored value array (double or float); products promote to double.
+    template <class F>
+    void with_values(F f) const {
+        if (values32) f(values32);
+        else f(values);
+    }
+    double value(int64_t s) const { return values32 ? static_cast<double>(values32[s]) : values[s]; }
+
     // indirect_multiply, sparse.hpp:185-235 (scatter along the secondary dimension).
     void indirect_multiply(const double* rhs, double* out) const {
+        with_values([&](const auto* vals) { indirect_impl(vals, rhs, out); });
+    }
+    template <class V>
+    void indirect_impl(const V* vals, const double* rhs, double* out) const {
         if (num_threads == 1) {
             std::fill(out, out + secondary_dim, 0.0);
             for (Index c = 0; c < primary_dim; ++c) {
                 const double val = rhs[c];
-                for (int64_t s = ptrs[c]; s < ptrs[c + 1]; ++s) out[indices[s]] += values[s] * val;
+                for (int64_t s = ptrs[c]; s < ptrs[c + 1]; ++s) out[indices[s]] += static_cast<double>(vals[s]) * val;
             }
             return;
         }
@@ -224,30 +238,35 @@ struct SparseMatrix : public Matrix {
             const auto& nz_ends = secondary_nonzero_boundaries[t + 1];
             for (Index c = 0; c < primary_dim; ++c) {
                 const double val = rhs[c];
-                for (int64_t s = nz_starts[c]; s < nz_ends[c]; ++s) optr[indices[s] - sstart] += values[s] * val;
+                for (int64_t s = nz_starts[c]; s < nz_ends[c]; ++s)
+                    optr[indices[s] - sstart] += static_cast<double>(vals[s]) * val;
             }
             if (t != 0) std::copy(optr, optr + (send - sstart), out + sstart);
         }
     }
 
     // column_dot_product, sparse.hpp:259-267.
-    double primary_dot(Index p, const double* rhs) const {
+    template <class V>
+    double primary_dot(const V* vals, Index p, const double* rhs) const {
         double dot = 0;
-        for (int64_t s = ptrs[p]; s < ptrs[p + 1]; ++s) dot += values[s] * rhs[indices[s]];
+        for (int64_t s = ptrs[p]; s < ptrs[p + 1]; ++s) dot += static_cast<double>(vals[s]) * rhs[indices[s]];
         return dot;
     }
 
     // direct_multiply, sparse.hpp:238-256 (gather along the primary dimension).
     void direct_multiply(const double* rhs, double* out) const {
-        if (num_threads == 1) {
-            for (Index c = 0; c < primary_dim; ++c) out[c] = primary_dot(c, rhs);
-            return;
-        }
+        with_values([&](const auto* vals) {
+            if (num_threads == 1) {
+                for (Index c = 0; c < primary_dim; ++c) out[c] = primary_dot(vals, c, rhs);
+                return;
+            }
 #pragma omp parallel num_threads(num_threads)
-        {
-            const int t = omp_get_thread_num();
-            for (Index c = primary_boundaries[t]; c < primary_boundaries[t + 1]; ++c) out[c] = primary_dot(c, rhs);
-        }
+            {
+                const int t = omp_get_thread_num();
+                for (Index c = primary_boundaries[t]; c < primary_boundaries[t + 1]; ++c)
+                    out[c] = primary_dot(vals, c, rhs);
+            }
+        });
     }
 
     // Layout dispatch, sparse.hpp:305-311 and :346-352.
@@ -263,8 +282,8 @@ struct SparseMatrix : public Matrix {
         std::fill(buf, buf + nr * nc, 0.0);
         for (Index p = 0; p < primary_dim; ++p) {
             for (int64_t s = ptrs[p]; s < ptrs[p + 1]; ++s) {
-                if (column_major) buf[p * nr + indices[s]] = values[s];
-                else buf[static_cast<Index>(indices[s]) * nr + p] = values[s];
+                if (column_major) buf[p * nr + indices[s]] = value(s);
+                else buf[static_cast<Index>(indices[s]) * nr + p] = value(s);
             }
         }
     }
@@ -362,19 +381,49 @@ inline double dot(const double* a, const double* b, Index n) {
 inline double norm(const double* a, Index n) { return std::sqrt(dot(a, a, n)); }
 
 // Threads used by the oracle's dense loops (CGS and rotations); 1 by default.
+// With more threads these loops run in parallel over fixed row blocks, so the
+// results do not depend on the thread count. (The reference's Eigen GEMV of
+// orthogonalize_vector is single-threaded; only its GEMMs use Eigen's threads.)
 static int g_dense_threads = 1;
 
+// Rows per block of the dense loops: the block of Q stays in L1/L2 while its
+// columns are combined.
+constexpr Index kDenseRowBlock = 512;
+
 // orthogonalize_vector, lanczos.hpp:17-21: tmp = Q[:, :ncols]^T v; v -= Q[:, :ncols] tmp.
+// The dot products sum each row block in row order, then the blocks in block
+// order; the update forms sum_j Q[r, j] tmp[j] in column order and subtracts it.
 void orthogonalize_vector(const Dense& Q, double* vec, Index ncols, double* tmp) {
     const Index L = Q.nr;
     const int nt = g_dense_threads;
+    const Index nblocks = (L + kDenseRowBlock - 1) / kDenseRowBlock;
+    std::vector<double> part(static_cast<size_t>(nblocks * ncols));
 #pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1 && L > 4096)
-    for (Index j = 0; j < ncols; ++j) tmp[j] = dot(Q.col(j), vec, L);
-#pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1 && L > 4096)
-    for (Index r = 0; r < L; ++r) {
+    for (Index b = 0; b < nblocks; ++b) {
+        const Index r0 = b * kDenseRowBlock, r1 = std::min(L, r0 + kDenseRowBlock);
+        for (Index j = 0; j < ncols; ++j) {
+            const double* q = Q.v.data() + j * L;
+            double s = 0;
+            for (Index r = r0; r < r1; ++r) s += q[r] * vec[r];
+            part[b * ncols + j] = s;
+        }
+    }
+    for (Index j = 0; j < ncols; ++j) {
         double s = 0;
-        for (Index j = 0; j < ncols; ++j) s += Q.v[j * L + r] * tmp[j];
-        vec[r] -= s;
+        for (Index b = 0; b < nblocks; ++b) s += part[b * ncols + j];
+        tmp[j] = s;
+    }
+#pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1 && L > 4096)
+    for (Index b = 0; b < nblocks; ++b) {
+        const Index r0 = b * kDenseRowBlock, r1 = std::min(L, r0 + kDenseRowBlock), nr = r1 - r0;
+        double acc[kDenseRowBlock];
+        for (Index i = 0; i < nr; ++i) acc[i] = 0;
+        for (Index j = 0; j < ncols; ++j) {
+            const double tj = tmp[j];
+            const double* q = Q.v.data() + j * L + r0;
+            for (Index i = 0; i < nr; ++i) acc[i] += q[i] * tj;
+        }
+        for (Index i = 0; i < nr; ++i) vec[r0 + i] -= acc[i];
     }
 }
 
@@ -619,15 +668,25 @@ void run_lanczos_bidiagonalization(const Matrix& mat, LanczosWorkspace& inter, D
 }
 
 // out[:, :k] = Q[:, :w] * R[:, :k]  (the rotation GEMMs of compute.hpp:268,279,302,305).
+// Each output entry sums over j in column order; rows are processed in blocks
+// that stay cache-resident while all k output columns are formed.
 void rotate(const Dense& Q, const Dense& R, Index k, Dense& out) {
     const Index L = Q.nr, w = Q.nc;
     const int nt = g_dense_threads;
+    const Index nblocks = (L + kDenseRowBlock - 1) / kDenseRowBlock;
 #pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1 && L > 4096)
-    for (Index r = 0; r < L; ++r) {
+    for (Index b = 0; b < nblocks; ++b) {
+        const Index r0 = b * kDenseRowBlock, r1 = std::min(L, r0 + kDenseRowBlock), nr = r1 - r0;
+        double acc[kDenseRowBlock];
         for (Index c = 0; c < k; ++c) {
-            double s = 0;
-            for (Index j = 0; j < w; ++j) s += Q.v[j * L + r] * R(j, c);
-            out.v[c * out.nr + r] = s;
+            for (Index i = 0; i < nr; ++i) acc[i] = 0;
+            for (Index j = 0; j < w; ++j) {
+                const double rj = R(j, c);
+                const double* q = Q.v.data() + j * L + r0;
+                for (Index i = 0; i < nr; ++i) acc[i] += q[i] * rj;
+            }
+            double* o = out.v.data() + c * out.nr + r0;
+            for (Index i = 0; i < nr; ++i) o[i] = acc[i];
         }
     }
 }
@@ -778,7 +837,7 @@ void column_stats_sparse(const SparseMatrix& m, bool center, bool scale, double*
     for (Index p = 0; p < m.primary_dim; ++p)
         for (int64_t s = m.ptrs[p]; s < m.ptrs[p + 1]; ++s) {
             const Index c = m.column_major ? p : m.indices[s];
-            sum[c] += m.values[s];
+            sum[c] += m.value(s);
             cnt[c] += 1;
         }
     std::vector<double> mean(nc, 0.0);
@@ -793,7 +852,7 @@ void column_stats_sparse(const SparseMatrix& m, bool center, bool scale, double*
         for (Index p = 0; p < m.primary_dim; ++p)
             for (int64_t s = m.ptrs[p]; s < m.ptrs[p + 1]; ++s) {
                 const Index c = m.column_major ? p : m.indices[s];
-                const double d = m.values[s] - mean[c];
+                const double d = m.value(s) - mean[c];
                 var[c] += d * d;
             }
         for (Index c = 0; c < nc; ++c) {
@@ -845,6 +904,7 @@ struct OracleMatrixSpec {
     const double* scale;
     int32_t scale_column;
     int32_t scale_divide;
+    const float* values32;   // FP32 values of a sparse base (kind 2) instead of `values`, or NULL
 };
 
 static thread_local std::string g_error;
@@ -861,7 +921,7 @@ struct Chain {
 static void build_chain(const OracleMatrixSpec* s, Chain& ch) {
     if (s->kind == 2) {
         ch.base.reset(new SparseMatrix(s->nrow, s->ncol, s->values, s->indices, s->pointers, s->column_major != 0,
-                                       s->num_threads < 1 ? 1 : s->num_threads));
+                                       s->num_threads < 1 ? 1 : s->num_threads, s->values32));
     } else {
         ch.base.reset(new DenseMatrix(s->nrow, s->ncol, s->dense, s->ld, s->kind == 1));
     }
@@ -934,7 +994,8 @@ int oracle_realize(const OracleMatrixSpec* s, double* out) {
 // Thread partitions of the ParallelSparseMatrix core (sparse.hpp:35-115).
 int oracle_sparse_partitions(const OracleMatrixSpec* s, int64_t* primary, int64_t* secondary, int64_t* secondary_nz) {
     try {
-        SparseMatrix m(s->nrow, s->ncol, s->values, s->indices, s->pointers, s->column_major != 0, s->num_threads);
+        SparseMatrix m(s->nrow, s->ncol, s->values, s->indices, s->pointers, s->column_major != 0, s->num_threads,
+                       s->values32);
         const int nt = s->num_threads;
         for (int t = 0; t <= nt; ++t) {
             primary[t] = m.primary_boundaries[t];

@@ -39,6 +39,19 @@ struct Mat {
     double operator()(std::ptrdiff_t r, std::ptrdiff_t c) const { return v[c * nr + r]; }
 };
 
+// A column-major view with an outer stride larger than its rows, like an Eigen
+// Map<MatrixXd, 0, OuterStride<>> or a Block of a larger matrix.
+struct StridedView {
+    const double* p = nullptr;
+    std::ptrdiff_t nr = 0, nc = 0, ld = 0;
+    const double* data() const { return p; }
+    std::ptrdiff_t rows() const { return nr; }
+    std::ptrdiff_t cols() const { return nc; }
+    std::ptrdiff_t outerStride() const { return ld; }
+    std::ptrdiff_t innerStride() const { return 1; }
+    double operator()(std::ptrdiff_t r, std::ptrdiff_t c) const { return p[c * ld + r]; }
+};
+
 // A caller's own Matrix subclass (Matrix/interface.hpp:141-223) with products
 // written by hand on the host; `fail` makes its multiply throw.
 class UserDense final : public irlba::Matrix<Vec, Mat> {
@@ -84,6 +97,15 @@ private:
     const Mat* my_a;
     bool my_fail;
 };
+
+// Options with the first `n` entries of `init` as the start vector.
+static irlba::Options<Vec> opt_block(const irlba::Options<Vec>& base, const Vec& init, std::ptrdiff_t n = 50) {
+    irlba::Options<Vec> o = base;
+    Vec v(n);
+    for (std::ptrdiff_t i = 0; i < n; ++i) v[i] = init.v[i];
+    o.initial = v;
+    return o;
+}
 
 static uint64_t lcg = 88172645463325252ull;
 static double next_normal() {
@@ -158,6 +180,25 @@ int main() {
     dump_vec("sparse_p", pd.data(), pd.size());
     dump_vec("center", center.data(), nc);
     dump_vec("scale", scale.data(), nc);
+
+    // The decorators read the caller's vectors when they are used, as the
+    // reference's pointers do: change the centre and scale after construction.
+    for (std::ptrdiff_t c = 0; c < nc; ++c) {
+        center[c] = 0.02 * c - 0.3;
+        scale[c] = 2.0 - 0.01 * c;
+    }
+    auto res3b = irlba::compute<Mat, Vec>(scl, 4, opt);
+    dump_vec("chain_changed_D", res3b.D.data(), res3b.D.size());
+    std::printf("\"chain_changed_iterations\": %d,\n", res3b.iterations);
+    dump_vec("center_changed", center.data(), nc);
+    dump_vec("scale_changed", scale.data(), nc);
+
+    // Dense input held with an outer stride (the top-left 100 x 50 block of A).
+    StridedView view{A.data(), 100, 50, nr};
+    irlba::SimpleMatrix<Vec, Mat, const StridedView*> strided(&view);
+    auto res7 = irlba::compute<Mat, Vec>(strided, 5, opt_block(opt, init));
+    dump_vec("strided_D", res7.D.data(), res7.D.size());
+    std::printf("\"strided_iterations\": %d,\n", res7.iterations);
 
     // Workspace multiply through the plug-in surface (interface.hpp:49, :87).
     auto w = scl.new_workspace();

@@ -50,8 +50,30 @@ def test_dropin_decorated_sparse(dropin_output, oracle_mod):
     orc = oracle_mod.compute(spec, 4, oracle_mod.options(initial=init))
     np.testing.assert_allclose(d["chain_D"], orc["D"], rtol=1e-10)
     assert d["chain_iterations"] == orc["iterations"]
-    np.testing.assert_allclose(d["chain_multiply_init"], oracle_mod.multiply(spec, init), rtol=1e-12, atol=1e-12)
+    # The centre and scale vectors changed after the decorators were built:
+    # the next compute uses the new contents (the reference reads them through
+    # its pointers, centered.hpp:46-52, scaled.hpp:52-69). The workspace
+    # multiply below ran after the change as well.
+    spec2 = oracle_mod.Spec.sparse(nr, nc, x, i, p, True, 1, center=np.array(d["center_changed"]),
+                                   scale=np.array(d["scale_changed"]))
+    orc2 = oracle_mod.compute(spec2, 4, oracle_mod.options(initial=init))
+    np.testing.assert_allclose(d["chain_changed_D"], orc2["D"], rtol=1e-10)
+    assert d["chain_changed_iterations"] == orc2["iterations"]
+    assert np.max(np.abs(np.array(d["chain_changed_D"]) - orc["D"]) / orc["D"]) > 1e-3
+    np.testing.assert_allclose(d["chain_multiply_init"], oracle_mod.multiply(spec2, init), rtol=1e-12, atol=1e-12)
     assert "cannot be greater than" in d["error_message"]
+
+
+def test_dropin_strided_dense(dropin_output, oracle_mod):
+    """A dense view with an outer stride (an Eigen Map with OuterStride, a
+    Block): the engine reads the view's elements, not a contiguous prefix."""
+    d = dropin_output
+    nr, nc = 120, 70
+    A = np.array(d["A_colmajor"]).reshape(nc, nr).T
+    init = np.array(d["init"])[:50]
+    orc = oracle_mod.compute(oracle_mod.Spec.dense(A[:100, :50].copy()), 5, oracle_mod.options(initial=init))
+    np.testing.assert_allclose(d["strided_D"], orc["D"], rtol=1e-10)
+    assert d["strided_iterations"] == orc["iterations"]
 
 
 def test_dropin_user_matrices(dropin_output, oracle_mod):
