@@ -55,7 +55,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparator")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default workload only: skip the 20k x 50k FP64, batched and adjoint sub-records")
     ap.add_argument("--cpu-restarts", type=int, default=2, help="restarts in the bounded CPU samples of the "
                     "secondary workloads")
     ap.add_argument("--workload", default="scrna_2k", choices=["scrna_2k", "batch", "adjoint", "csc20k"],
@@ -63,6 +65,8 @@ def parse():
                          "launch; adjoint: truncated-SVD forward + backward; csc20k: plain FP64 PCA of the "
                          "20,000-gene x 50,000-cell matrix")
     ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--spmv-shape", type=int, default=None,
+                    help="SpMV launch shape of this run's FP32 matrices (see cppirlba_gb300.set_spmv_shape)")
     return ap.parse_args()
 
 
@@ -351,8 +355,7 @@ def run_batch(args):
         out["cpu_baseline"] = {"value": est, "unit": "s", "cores": threads, "kind": "port",
                                "sample": "FP64 oracle pca() (CppIrlba algorithm restated, OpenMP) of 5 matrices at "
                                          "size quantiles (%.1f s), scaled by total nnz / sample nnz" % t_cpu}
-    if rank == 0:
-        print(json.dumps(out), flush=True)
+    return out
 
 
 def run_adjoint(args):
@@ -435,8 +438,7 @@ def run_adjoint(args):
         out["cpu_baseline"] = {"value": dt, "unit": "s", "cores": os.cpu_count() or 1, "kind": "port",
                                "sample": "numpy oracle: full LAPACK SVD + F-matrix and rank-k projection terms "
                                          "(the exact complement solve is O(m^3) there and is not timed)"}
-    if rank == 0:
-        print(json.dumps(out), flush=True)
+    return out
 
 
 def run_csc20k(args):
@@ -538,20 +540,32 @@ def run_csc20k(args):
         out["e2e"] = {"value": reduce_max(statistics.median(times), "cuda"), "unit": "s",
                       "h2d_bytes_per_step": (h1 - h0) // len(times), "d2h_bytes_per_step": (d1 - d0) // len(times)}
     if not args.no_cpu and rank == 0:
+        # One full FP64 oracle solve to tolerance (measured), also the parity
+        # check of the GPU result at this size.
         import oracle
         threads = os.cpu_count() or 1
         spec = oracle.Spec.sparse(m, n, inp.val, inp.idx, inp.ptr, inp.column_major, threads)
         t1 = time.perf_counter()
         r = oracle.pca(spec, True, True, NUMBER, oracle.options(initial=init, convergence_tolerance=TOL),
-                       dense_threads=threads, max_restarts=args.cpu_restarts)
+                       dense_threads=threads)
         dt = time.perf_counter() - t1
-        per_step = dt / max(r["lanczos_steps"], 1)
-        out["cpu_baseline"] = {"value": per_step * st["lanczos_steps"], "unit": "s", "cores": threads, "kind": "port",
-                               "sample": "FP64 oracle pca() column stats + first %d restarts (%d Lanczos steps) in "
-                                         "%.2f s, scaled by the %d Lanczos steps to tol" %
-                                         (args.cpu_restarts, r["lanczos_steps"], dt, st["lanczos_steps"])}
-    if rank == 0:
-        print(json.dumps(out), flush=True)
+        D_gpu = np.sqrt(dD.cpu().numpy() * (m - 1))
+        D_orc = np.sqrt(np.asarray(r["variances"]) * (m - 1))
+        out["cpu_baseline"] = {"value": dt, "unit": "s", "cores": threads, "kind": "port",
+                               "sample": "one full FP64 oracle pca() to tol, measured: %d restarts, %d Lanczos "
+                                         "steps, converged %s" % (r["iterations"], r["lanczos_steps"], r["converged"])}
+        out["D_max_rel_err_vs_fp64_oracle"] = float(np.max(np.abs(D_gpu - D_orc) / D_orc))
+        out["restarts_equal_oracle"] = iters == r["iterations"]
+    return out
+
+
+def sub_args(args):
+    """Step counts of the secondary workloads inside the default run: a few
+    timed steps each, so the whole default run stays within minutes."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = max(1, min(args.steps, 3))
+    sub.warmup = max(1, min(args.warmup, 1))
+    return sub
 
 
 def main():
@@ -559,14 +573,11 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    if args.workload == "batch":
-        run_batch(args)
-        return
-    if args.workload == "adjoint":
-        run_adjoint(args)
-        return
-    if args.workload == "csc20k":
-        run_csc20k(args)
+    standalone = {"batch": run_batch, "adjoint": run_adjoint, "csc20k": run_csc20k}
+    if args.workload in standalone:
+        out = standalone[args.workload](args)
+        if dist_setup()[1] == 0:
+            print(json.dumps(out), flush=True)
         return
     world, rank, local = dist_setup()
     import torch
@@ -585,6 +596,8 @@ def main():
         return reduce_max(x, "cuda")
 
     eng.load_library()
+    if args.spmv_shape is not None:
+        eng.set_spmv_shape(args.spmv_shape)
     t_gen = time.perf_counter()
     inp = make_input(args)
     t_gen = time.perf_counter() - t_gen
@@ -765,7 +778,8 @@ def main():
                            "lanczos_steps": r64["stats"]["lanczos_steps"], "converged": r64["converged"],
                            "kernel_ms": {k: v["ms"] for k, v in pr64.items()},
                            "speedup_fp32_form": ms64 / ms_per_step,
-                           "fp32_D_max_rel_err_vs_fp64": float(np.max(np.abs(D32 - D64) / D64))}
+                           "fp32_D_max_rel_err_vs_fp64": float(np.max(np.abs(np.sqrt(D32) - np.sqrt(D64)) /
+                                                                     np.sqrt(D64)))}
         mat64.close()
 
     # The FP64 oracle on the host cores: one full solve to tolerance (measured),
@@ -775,16 +789,31 @@ def main():
         log("cpu oracle solve on %d threads" % threads)
         dt, r = cpu_solve(inp, init, threads)
         log("cpu oracle %.1f s, %d restarts, %d steps" % (dt, r["iterations"], r["lanczos_steps"]))
-        # pca variances are D^2 / (m - 1): compare singular values.
+        # pca variances are D^2 / (m - 1) (pca.hpp:131-136), on both sides:
+        # compare singular values.
         D_orc = np.sqrt(np.asarray(r["variances"]) * (m - 1))
+        D32s = np.sqrt(D32 * (m - 1))
         out["cpu_baseline"] = {"value": dt, "unit": "s", "cores": threads, "kind": "port",
                                "sample": "one full FP64 oracle pca() to tol, measured (CppIrlba algorithm restated, "
                                          "OpenMP): %d restarts, %d Lanczos steps, converged %s" %
                                          (r["iterations"], r["lanczos_steps"], r["converged"])}
-        out["fp32_D_max_rel_err_vs_fp64_oracle"] = float(np.max(np.abs(D32 - D_orc) / D_orc))
+        out["fp32_D_max_rel_err_vs_fp64_oracle"] = float(np.max(np.abs(D32s - D_orc) / D_orc))
         if "fp64_gpu" in out:
-            out["fp64_gpu"]["D_max_rel_err_vs_fp64_oracle"] = float(np.max(np.abs(D64 - D_orc) / D_orc))
+            D64s = np.sqrt(D64 * (m - 1))
+            out["fp64_gpu"]["D_max_rel_err_vs_fp64_oracle"] = float(np.max(np.abs(D64s - D_orc) / D_orc))
             out["fp64_gpu"]["restarts_equal_oracle"] = out["fp64_gpu"]["restarts"] == r["iterations"]
+
+    # The other benchmark configurations as sub-records of the same line, each
+    # with its own roofline, clocks and CPU baseline (a few steps each).
+    if not args.no_extra and world == 1:
+        sub = sub_args(args)
+        for key, fn in (("fp64_pca_20k_x_50k", run_csc20k), ("batched_256", run_batch),
+                        ("adjoint_4096x1024", run_adjoint)):
+            log("sub-record %s" % key)
+            try:
+                out[key] = fn(sub)
+            except Exception as exc:  # a failed sub-record is reported, not fatal
+                out[key] = {"error": "%s: %s" % (type(exc).__name__, exc)}
 
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -153,6 +153,7 @@ def load_library():
                                             ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]),
         "irlba_gb300_set_profiling": (None, [i32]),
         "irlba_gb300_set_device_ingest": (None, [i32]),
+        "irlba_gb300_set_spmv_shape": (None, [i32]),
         "irlba_gb300_set_staging": (None, [i64, i64]),
         "irlba_gb300_last_profile": (None, [pd, ctypes.POINTER(i64)]),
         "irlba_gb300_launch_count": (i64, []),
@@ -584,6 +585,13 @@ def device_count():
 def set_device_ingest(on):
     """Build sparse matrices' device layout on the GPU (default) or on the host."""
     load_library().irlba_gb300_set_device_ingest(int(bool(on)))
+
+
+def set_spmv_shape(shape):
+    """Launch shape of the sparse products of FP32-form matrices created
+    afterwards: 0 = 256-thread CTAs, 1 = 256 threads six per SM, 2 (default) =
+    512 threads three per SM."""
+    load_library().irlba_gb300_set_spmv_shape(int(shape))
 
 
 def set_staging(min_bytes=16 << 20, slice_bytes=8 << 20):

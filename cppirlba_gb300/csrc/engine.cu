@@ -26,6 +26,9 @@
 #include <type_traits>
 #include <vector>
 
+#include <dlfcn.h>
+#include <cusolverDn.h>
+
 #include "host.hpp"
 #include "matrix.hpp"
 
@@ -154,6 +157,15 @@ static void transpose_host(const HostCompressed& in, HostCompressed& out) {
 // Relative cost of a segment against one nonzero when balancing CTAs.
 constexpr int64_t kSegCost = 8;
 
+// Launch shape of the SpMV kernel for FP32 staged plans of matrices created
+// from now on (see spmv_shape_threads): 2, 512-thread CTAs three per SM, is
+// the default (the fastest measured on the 2,000 x 1.3M FP32 workload: more
+// resident warps, more loads in flight); FP64 and unstaged plans use shape 0.
+static int g_spmv_shape = 2;
+static int plan_shape(bool staged, bool store_f64, bool x_f64) {
+    return (staged && !store_f64 && !x_f64) ? g_spmv_shape : 0;
+}
+
 static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirPlan& plan) {
     TRACE("build_plan: %lld x %lld, nnz %lld", (long long)h.rows, (long long)h.cols, (long long)h.ptr[h.rows]);
     const DeviceInfo& di = device_info();
@@ -237,7 +249,8 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
         const double vecs = avg / (store_f64 ? 2.0 : 4.0);
         d.group_lanes = vecs >= 96 ? 32 : vecs >= 24 ? 16 : vecs >= 6 ? 8 : 4;
     }
-    const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes, d.group_lanes);
+    d.shape = plan_shape(staged, store_f64, x_f64);
+    const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes, d.group_lanes, d.shape);
     TRACE("build_plan: %d blocks per SM", per_sm);
     int64_t nblocks = static_cast<int64_t>(di.sms) * per_sm;
     const int64_t total_cost = nnz + kSegCost * nseg;
@@ -331,7 +344,8 @@ static void build_plan_device(const DevCompressed& h, bool store_f64, bool x_f64
         const double vecs = avg / (store_f64 ? 2.0 : 4.0);
         d.group_lanes = vecs >= 96 ? 32 : vecs >= 24 ? 16 : vecs >= 6 ? 8 : 4;
     }
-    const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes, d.group_lanes);
+    d.shape = plan_shape(staged, store_f64, x_f64);
+    const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes, d.group_lanes, d.shape);
     int64_t nblocks = static_cast<int64_t>(di.sms) * per_sm;
     const int64_t total_cost = nnz + kSegCost * nseg;
     nblocks = std::max<int64_t>(1, std::min<int64_t>(nblocks, std::max<int64_t>(1, total_cost / 2048)));
@@ -460,6 +474,9 @@ static void operator_product(const BaseMatrix& A, bool adjoint, const T* x, T* y
     }
     if (rc != 0) invalid("user-defined product failed (status " + std::to_string(rc) + ")");
 }
+
+static void gesvd_device(const double* A, int64_t mm, int64_t nn, double* U, double* S, double* V,
+                         cudaStream_t stream);
 
 template <typename T>
 struct Engine {
@@ -737,6 +754,23 @@ struct Engine {
         }
     }
 
+    // The restart step (compute.hpp:225-293). Working subspaces above 1024
+    // (beyond the one-CTA Jacobi kernel's shared arrays) take the SVD of B
+    // from cuSOLVER, after checking that the Lanczos run was not aborted, and
+    // the rest of the step from the tail kernel.
+    void restart(const RestartArgs& ra, size_t smem) {
+        if (ra.work <= 1024) {
+            launch_restart(ra, stream, smem);
+            return;
+        }
+        Ctrl h;
+        CUDA_TRY(d2h_async(&h, ctrl, sizeof(Ctrl), stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        if (h.abort) return;
+        gesvd_device(ra.B, ra.work, ra.work, ra.BU, ra.BS, ra.BV, stream);
+        launch_restart_tail(ra, stream);
+    }
+
     struct Result {
         bool converged = false;
         int iterations = 0;
@@ -748,9 +782,6 @@ struct Engine {
         const int64_t smaller = std::min(m, n);
         const int64_t w64 = (requested >= smaller) ? smaller : requested + std::min<int64_t>(smaller - requested, opt.extra_work);
         if (w64 == 0) invalid("number of requested dimensions must be positive");
-        if (w64 > 128)
-            throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
-                        "the GPU engine supports a working subspace (number + extra_work) of at most 128");
         work = static_cast<int>(w64);
         ldv = round_up(std::max<int64_t>(n, 1), 32);
         ldw = round_up(std::max<int64_t>(m, 1), 32);
@@ -851,7 +882,7 @@ struct Engine {
             if (overlap) CUDA_TRY(cudaEventRecord(ev_f, stream));
             {
                 Scoped sc(timer, kTRestart);
-                launch_restart(ra, stream, restart_smem);
+                restart(ra, restart_smem);
             }
             if (overlap) {
                 // Behind the restart kernel: Wn = A'F on the side stream.
@@ -877,7 +908,7 @@ struct Engine {
                 lanczos(k, true, eng, matvecs);
                 {
                     Scoped sc(timer, kTRestart);
-                    launch_restart(ra, stream, restart_smem);
+                    restart(ra, restart_smem);
                 }
                 sync_ctrl(h);
                 if (h.null_start) throw Error(IRLBA_GB300_ERROR_NUMERICAL, "starting vector near the null space of the input matrix");
@@ -1008,14 +1039,127 @@ __global__ void scale_columns_kernel(double* A, int64_t m, int64_t r, const doub
 }
 
 // Exact SVD (compute.hpp:30-46) on the device: realize, then one-sided Jacobi.
+// cuSOLVER's dense SVD (cusolverDnDgesvd), loaded on first use for SVDs
+// whose smaller dimension is above what the one-CTA Jacobi kernel holds (1024
+// columns); the engine library does not link it.
+struct CusolverApi {
+    decltype(&cusolverDnCreate) create = nullptr;
+    decltype(&cusolverDnDestroy) destroy = nullptr;
+    decltype(&cusolverDnSetStream) set_stream = nullptr;
+    decltype(&cusolverDnDgesvd_bufferSize) buffer_size = nullptr;
+    decltype(&cusolverDnDgesvd) gesvd = nullptr;
+    bool ok = false;
+};
+static const CusolverApi& cusolver_api() {
+    static const CusolverApi api = [] {
+        CusolverApi a;
+        void* h = nullptr;
+        for (const char* name : {"libcusolver.so", "libcusolver.so.12", "libcusolver.so.11",
+                                 "/usr/local/cuda/lib64/libcusolver.so"}) {
+            h = dlopen(name, RTLD_NOW | RTLD_LOCAL);
+            if (h) break;
+        }
+        if (!h) return a;
+        a.create = reinterpret_cast<decltype(a.create)>(dlsym(h, "cusolverDnCreate"));
+        a.destroy = reinterpret_cast<decltype(a.destroy)>(dlsym(h, "cusolverDnDestroy"));
+        a.set_stream = reinterpret_cast<decltype(a.set_stream)>(dlsym(h, "cusolverDnSetStream"));
+        a.buffer_size = reinterpret_cast<decltype(a.buffer_size)>(dlsym(h, "cusolverDnDgesvd_bufferSize"));
+        a.gesvd = reinterpret_cast<decltype(a.gesvd)>(dlsym(h, "cusolverDnDgesvd"));
+        a.ok = a.create && a.destroy && a.set_stream && a.buffer_size && a.gesvd;
+        return a;
+    }();
+    return api;
+}
+
+// Canonical signs of a thin SVD (the largest-magnitude entry of each V column
+// positive, the first one on ties; the U column follows), the convention of
+// the Jacobi kernels and the oracle. One CTA of 256 threads per column.
+__global__ void canonical_signs_kernel(double* U, int64_t m, double* V, int64_t n, int64_t ncols) {
+    __shared__ double best_v[32];
+    __shared__ int64_t best_i[32];
+    __shared__ bool flip;
+    const int64_t j = blockIdx.x;
+    if (j >= ncols) return;
+    double* v = V + j * n;
+    double best = -1.0;
+    int64_t arg = n;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double a = fabs(v[i]);
+        if (a > best) {
+            best = a;
+            arg = i;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int64_t oa = __shfl_xor_sync(0xffffffffu, arg, o);
+        if (ob > best || (ob == best && oa < arg)) {
+            best = ob;
+            arg = oa;
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        best_v[warp] = best;
+        best_i[warp] = arg;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = -1.0;
+        int64_t a = n;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w)
+            if (best_v[w] > b || (best_v[w] == b && best_i[w] < a)) {
+                b = best_v[w];
+                a = best_i[w];
+            }
+        flip = a < n && v[a] < 0;
+    }
+    __syncthreads();
+    if (!flip) return;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) v[i] = -v[i];
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) U[i + j * m] = -U[i + j * m];
+}
+
+// Thin SVD of a tall column-major mm x nn matrix (copied first) by cuSOLVER:
+// U (mm x nn), S (nn, descending), V (nn x nn), canonical signs.
+static void gesvd_device(const double* A, int64_t mm, int64_t nn, double* U, double* S, double* V,
+                         cudaStream_t stream) {
+    const CusolverApi& api = cusolver_api();
+    if (!api.ok)
+        throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
+                    "an SVD with more than 1024 columns needs cuSOLVER, which could not be loaded");
+    if (mm > INT32_MAX || nn > INT32_MAX) invalid("matrix too large for the dense SVD");
+    cusolverDnHandle_t h = nullptr;
+    if (api.create(&h) != CUSOLVER_STATUS_SUCCESS) throw Error(IRLBA_GB300_ERROR_CUDA, "cusolverDnCreate failed");
+    struct Guard {
+        const CusolverApi& a;
+        cusolverDnHandle_t h;
+        ~Guard() { a.destroy(h); }
+    } guard{api, h};
+    api.set_stream(h, stream);
+    int lwork = 0;
+    if (api.buffer_size(h, static_cast<int>(mm), static_cast<int>(nn), &lwork) != CUSOLVER_STATUS_SUCCESS)
+        throw Error(IRLBA_GB300_ERROR_CUDA, "cusolverDnDgesvd_bufferSize failed");
+    DevBuf Acopy(sizeof(double) * mm * nn), VT(sizeof(double) * nn * nn), work(sizeof(double) * std::max(lwork, 1)),
+        rwork(sizeof(double) * std::max<int64_t>(nn, 1)), info(sizeof(int));
+    CUDA_TRY(cudaMemcpyAsync(Acopy.ptr, A, sizeof(double) * mm * nn, cudaMemcpyDeviceToDevice, stream));
+    const cusolverStatus_t st =
+        api.gesvd(h, 'S', 'S', static_cast<int>(mm), static_cast<int>(nn), Acopy.as<double>(), static_cast<int>(mm), S,
+                  U, static_cast<int>(mm), VT.as<double>(), static_cast<int>(nn), work.as<double>(), lwork,
+                  rwork.as<double>(), info.as<int>());
+    if (st != CUSOLVER_STATUS_SUCCESS) throw Error(IRLBA_GB300_ERROR_CUDA, "cusolverDnDgesvd failed");
+    int hinfo = 0;
+    CUDA_TRY(cudaMemcpyAsync(&hinfo, info.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (hinfo != 0) throw Error(IRLBA_GB300_ERROR_NUMERICAL, "the dense SVD did not converge");
+    transpose_kernel<<<152 * 8, 256, 0, stream>>>(VT.as<double>(), nn, nn, V); count_launch();
+    canonical_signs_kernel<<<static_cast<unsigned>(nn), 256, 0, stream>>>(U, mm, V, nn, nn); count_launch();
+    CUDA_TRY(cudaStreamSynchronize(stream));
+}
+
 static void exact_device(const Chain& ch, int64_t requested, double* dU, double* dV, double* dD,
                          cudaStream_t stream) {
     const int64_t m = ch.base->nrow, n = ch.base->ncol;
-    // The one-CTA Jacobi kernel keeps per-column norms and the sort order of
-    // at most 1024 columns in shared memory.
-    if (std::min(m, n) > 1024)
-        throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
-                    "the exact SVD on the device supports a smaller matrix dimension of at most 1024");
     DevBuf dense(sizeof(double) * std::max<int64_t>(m * n, 1));
     realize_device(ch, dense.as<double>(), stream);
     const bool tall = m >= n;
@@ -1027,11 +1171,18 @@ static void exact_device(const Chain& ch, int64_t requested, double* dU, double*
         transpose_kernel<<<152 * 8, 256, 0, stream>>>(dense.as<double>(), m, n, At.as<double>()); count_launch();
         Ain = At.as<double>();
     }
-    DevBuf U(sizeof(double) * mm * nn), S(sizeof(double) * nn), V(sizeof(double) * nn * nn),
-        scratch(sizeof(double) * (mm * nn + nn * nn)), ctrlb(sizeof(Ctrl));
-    CUDA_TRY(cudaMemsetAsync(ctrlb.ptr, 0, sizeof(Ctrl), stream));
-    launch_dense_svd(Ain, mm, nn, U.as<double>(), S.as<double>(), V.as<double>(), scratch.as<double>(),
-                     ctrlb.as<Ctrl>(), stream);
+    DevBuf U(sizeof(double) * mm * nn), S(sizeof(double) * nn), V(sizeof(double) * nn * nn);
+    if (nn > 1024) {
+        // The one-CTA Jacobi kernel keeps per-column norms and the sort order
+        // of at most 1024 columns in shared memory.
+        gesvd_device(Ain, mm, nn, U.as<double>(), S.as<double>(), V.as<double>(), stream);
+    } else {
+        DevBuf scratch(sizeof(double) * (mm * nn + nn * nn)), ctrlb(sizeof(Ctrl));
+        CUDA_TRY(cudaMemsetAsync(ctrlb.ptr, 0, sizeof(Ctrl), stream));
+        launch_dense_svd(Ain, mm, nn, U.as<double>(), S.as<double>(), V.as<double>(), scratch.as<double>(),
+                         ctrlb.as<Ctrl>(), stream);
+        CUDA_TRY(cudaStreamSynchronize(stream));
+    }
     CUDA_TRY(cudaMemcpyAsync(dD, S.ptr, sizeof(double) * requested, cudaMemcpyDeviceToDevice, stream));
     // tall: A = U S V^T, U is m x n. wide: A^T = U' S V'^T, so U = V' (m x m), V = U' (n x m).
     const double* Usrc = tall ? U.as<double>() : V.as<double>();
@@ -1362,6 +1513,7 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
 }
 
 void irlba_gb300_set_device_ingest(int32_t on) { g_device_ingest = on != 0; }
+void irlba_gb300_set_spmv_shape(int32_t shape) { g_spmv_shape = shape >= 0 && shape <= 2 ? shape : 2; }
 
 irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, const void* values,
                                                    irlba_gb300_value_type value_type, int64_t ld, int32_t row_major,

@@ -33,7 +33,10 @@ struct DirPlanDev {
     const int64_t* block_seg = nullptr;  // nblocks + 1 segment boundaries per CTA
     size_t smem_bytes = 0;
     int32_t group_lanes = 32;            // lanes per segment: 4, 8, 16 or 32
+    int32_t shape = 0;                   // launch shape of the kernel (see spmv_shape_threads)
 };
+// Threads per CTA of an SpMV launch shape.
+int spmv_shape_threads(int shape);
 
 // Fused prologue/epilogue of a matvec (deferred centring and scaling, and the
 // Lanczos axpy). With acc the raw sparse product of row r:
@@ -67,7 +70,7 @@ void launch_epilogue(T* y, int64_t nrows, const Epilogue<T>& e, const int32_t* a
 
 // Launch configuration helpers (dynamic shared-memory limits, occupancy, grids).
 cudaError_t spmv_configure(size_t max_smem);
-int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group);
+int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group, int shape = 0);
 cudaError_t rotate_configure(size_t max_smem);
 int cgs_update_grid(int64_t L);
 int cgs_dot_grid(int64_t L);
@@ -150,6 +153,8 @@ struct RestartArgs {
     Ctrl* ctrl;
 };
 void launch_restart(const RestartArgs& a, cudaStream_t stream, size_t max_smem);
+// The convergence test, update_k and the rebuild of B alone, given BS, BU, BV.
+void launch_restart_tail(const RestartArgs& a, cudaStream_t stream);
 // out[i] = the restart kernel's update_k(args[4i], args[4i+1], args[4i+2], args[4i+3])
 // (k, requested, n_converged, work), compute.hpp:78-111.
 void launch_update_k(const int32_t* args, int64_t count, int32_t* out, cudaStream_t stream);

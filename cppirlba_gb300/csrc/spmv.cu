@@ -34,8 +34,8 @@ __device__ __forceinline__ T apply_epilogue(T v, int64_t r, const Epilogue<T>& e
 
 // G lanes per segment (32 / G segments per warp), chosen per plan from the
 // average segment length so that short rows share the per-segment bookkeeping.
-template <typename VT, typename T, bool STAGED, int G>
-__global__ void __launch_bounds__(kSpmvThreads) spmv_kernel(const DirPlanDev p, const T* __restrict__ x,
+template <typename VT, typename T, bool STAGED, int G, int TH = kSpmvThreads, int MINB = 1>
+__global__ void __launch_bounds__(TH, MINB) spmv_kernel(const DirPlanDev p, const T* __restrict__ x,
                                                             T* __restrict__ y, T* __restrict__ partial,
                                                             const Epilogue<T> e, const int32_t* abort) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -157,23 +157,32 @@ int grid_for(int64_t n, int threads, int cap) {
 }  // namespace
 
 // Calls f with the kernel instantiation for (value type, vector type, staged,
-// group lanes).
+// group lanes, launch shape). Launch shapes (FP32 staged plans with FP32
+// vectors; the others use shape 0): 0 = 256 threads; 1 = 256 threads,
+// registers capped for six CTAs per SM; 2 = 512 threads, registers capped for
+// three CTAs per SM.
 template <typename T, typename F>
-static void with_spmv_kernel(bool vf64, bool staged, int group, F f) {
-#define IRLBA_SPMV_G(VT, ST)                                    \
-    switch (group) {                                            \
-        case 4: f(spmv_kernel<VT, T, ST, 4>); break;            \
-        case 8: f(spmv_kernel<VT, T, ST, 8>); break;            \
-        case 16: f(spmv_kernel<VT, T, ST, 16>); break;          \
-        default: f(spmv_kernel<VT, T, ST, 32>); break;          \
+static void with_spmv_kernel(bool vf64, bool staged, int group, F f, int shape = 0) {
+#define IRLBA_SPMV_G(VT, ST, TH, MB)                                    \
+    switch (group) {                                                    \
+        case 4: f(spmv_kernel<VT, T, ST, 4, TH, MB>); break;            \
+        case 8: f(spmv_kernel<VT, T, ST, 8, TH, MB>); break;            \
+        case 16: f(spmv_kernel<VT, T, ST, 16, TH, MB>); break;          \
+        default: f(spmv_kernel<VT, T, ST, 32, TH, MB>); break;          \
     }
     if (vf64) {
-        if (staged) { IRLBA_SPMV_G(double, true) } else { IRLBA_SPMV_G(double, false) }
+        if (staged) { IRLBA_SPMV_G(double, true, 256, 1) } else { IRLBA_SPMV_G(double, false, 256, 1) }
+    } else if (!staged || !std::is_same<T, float>::value || shape == 0) {
+        if (staged) { IRLBA_SPMV_G(float, true, 256, 1) } else { IRLBA_SPMV_G(float, false, 256, 1) }
+    } else if (shape == 1) {
+        IRLBA_SPMV_G(float, true, 256, 6)
     } else {
-        if (staged) { IRLBA_SPMV_G(float, true) } else { IRLBA_SPMV_G(float, false) }
+        IRLBA_SPMV_G(float, true, 512, 3)
     }
 #undef IRLBA_SPMV_G
 }
+
+int spmv_shape_threads(int shape) { return shape == 2 ? 512 : 256; }
 
 template <typename T>
 void launch_spmv(const DirPlanDev& p, const T* x, T* y, T* partial, const Epilogue<T>& e, const int32_t* abort,
@@ -181,9 +190,10 @@ void launch_spmv(const DirPlanDev& p, const T* x, T* y, T* partial, const Epilog
     if (p.nrows == 0) return;
     if (p.nblocks > 0) {
         const size_t smem = p.staged ? p.smem_bytes : 0;
+        const int th = spmv_shape_threads(p.shape);
         with_spmv_kernel<T>(p.val_f64 != 0, p.staged != 0, p.group_lanes, [&](auto kernel) {
-            kernel<<<p.nblocks, kSpmvThreads, smem, stream>>>(p, x, y, partial, e, abort);
-        });
+            kernel<<<p.nblocks, th, smem, stream>>>(p, x, y, partial, e, abort);
+        }, p.shape);
         count_launch();
     }
     if (p.npanels > 1) {
@@ -217,6 +227,8 @@ cudaError_t spmv_configure(size_t max_smem) {
     };
     for (int g = 4; g <= 32; g *= 2) {
         with_spmv_kernel<float>(false, true, g, set);
+        with_spmv_kernel<float>(false, true, g, set, 1);
+        with_spmv_kernel<float>(false, true, g, set, 2);
         with_spmv_kernel<float>(true, true, g, set);
         with_spmv_kernel<double>(false, true, g, set);
         with_spmv_kernel<double>(true, true, g, set);
@@ -224,13 +236,14 @@ cudaError_t spmv_configure(size_t max_smem) {
     return err;
 }
 
-int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group) {
+int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group, int shape) {
     int nb = 0;
+    const int th = spmv_shape_threads(shape);
     auto occ = [&](auto kernel) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kSpmvThreads, staged ? smem : 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, th, staged ? smem : 0);
     };
-    if (tf64) with_spmv_kernel<double>(vf64, staged, group, occ);
-    else with_spmv_kernel<float>(vf64, staged, group, occ);
+    if (tf64) with_spmv_kernel<double>(vf64, staged, group, occ, shape);
+    else with_spmv_kernel<float>(vf64, staged, group, occ, shape);
     return nb < 1 ? 1 : nb;
 }
 

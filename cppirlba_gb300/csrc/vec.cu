@@ -120,7 +120,9 @@ __global__ void __launch_bounds__(kThreads) cgs_update_kernel(const T* __restric
     __shared__ double red[32];
     __shared__ bool is_last;
     if (ctrl->abort) return;
-    for (int j = threadIdx.x; j < c; j += blockDim.x) ts[j] = static_cast<T>(t[j]);
+    // The first kMaxCols coefficients are staged; any beyond are read from t.
+    const int cs = c < kMaxCols ? c : kMaxCols;
+    for (int j = threadIdx.x; j < cs; j += blockDim.x) ts[j] = static_cast<T>(t[j]);
     __syncthreads();
 
     double sq = 0;
@@ -129,14 +131,15 @@ __global__ void __launch_bounds__(kThreads) cgs_update_kernel(const T* __restric
         T s = 0;
         const T* __restrict__ q = Q + r;
         int j = 0;
-        for (; j + 3 < c; j += 4) {
+        for (; j + 3 < cs; j += 4) {
             const T q0 = q[j * ldq], q1 = q[(j + 1) * ldq], q2 = q[(j + 2) * ldq], q3 = q[(j + 3) * ldq];
             s += q0 * ts[j];
             s += q1 * ts[j + 1];
             s += q2 * ts[j + 2];
             s += q3 * ts[j + 3];
         }
-        for (; j < c; ++j) s += q[j * ldq] * ts[j];
+        for (; j < cs; ++j) s += q[j * ldq] * ts[j];
+        for (; j < c; ++j) s += q[j * ldq] * static_cast<T>(__ldg(t + j));
         const T nv = v[r] - s;
         v[r] = nv;
         sq += static_cast<double>(nv) * static_cast<double>(nv);
@@ -371,9 +374,90 @@ __global__ void __launch_bounds__(256) rotate_f32_gemm_kernel(const float* Q, in
     }
 }
 
+// Rotations with more than 128 basis columns: tmp (rows x k, ld rows) =
+// Q[r0 : r0 + rows, :w] R[:w, :k] with 32 x 32 output tiles and 32-column
+// steps through w in shared memory; then tmp is copied over out (in place is
+// safe: every read of the chunk's rows happens in the product kernel).
+template <typename T>
+__global__ void __launch_bounds__(256) rotate_chunk_kernel(const T* __restrict__ Q, int64_t r0, int64_t rows,
+                                                           int64_t ldq, int32_t w, const double* __restrict__ R,
+                                                           int32_t ldr, int32_t k, T* __restrict__ tmp) {
+    __shared__ T Qs[32][33];
+    __shared__ T Rs[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;      // 32 x 8 threads, 4 outputs each
+    const int64_t rb = static_cast<int64_t>(blockIdx.x) * 32;
+    const int cb = blockIdx.y * 32;
+    T acc[4] = {0, 0, 0, 0};
+    for (int j0 = 0; j0 < w; j0 += 32) {
+        for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
+            const int a = t % 32, b = t / 32;                          // a: row / j, b: j / column
+            const int64_t r = rb + a;
+            Qs[b][a] = (r < rows && j0 + b < w) ? Q[r0 + r + static_cast<int64_t>(j0 + b) * ldq] : T(0);
+            Rs[b][a] = (j0 + a < w && cb + b < k) ? static_cast<T>(R[(j0 + a) + static_cast<int64_t>(cb + b) * ldr])
+                                                  : T(0);
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) {
+            const T q = Qs[j][tx];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[u] += q * Rs[ty + 8 * u][j];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int64_t r = rb + tx;
+        const int c = cb + ty + 8 * u;
+        if (r < rows && c < k) tmp[r + static_cast<int64_t>(c) * rows] = acc[u];
+    }
+}
+
+template <typename T, typename O>
+__global__ void rotate_chunk_store_kernel(const T* __restrict__ tmp, int64_t r0, int64_t rows, int32_t k, O* out,
+                                          int64_t ldo, const T* __restrict__ fcol, const double* fnorm) {
+    const T finv = fcol ? static_cast<T>(1.0 / *fnorm) : T(0);
+    const int64_t total = rows * (k + (fcol ? 1 : 0));
+    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = e % rows, c = e / rows;
+        if (c < k) out[r0 + r + c * ldo] = static_cast<O>(tmp[r + c * rows]);
+        else out[r0 + r + static_cast<int64_t>(k) * ldo] = static_cast<O>(fcol[r0 + r] * finv);
+    }
+}
+
+template <typename T, typename O>
+static void rotate_wide(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                        O* out, int64_t ldo, const T* fcol, const double* fnorm, cudaStream_t stream) {
+    if (L == 0 || (k == 0 && !fcol)) return;
+    // Chunks of rows whose product fits a 256 MB stream-ordered temporary.
+    const int64_t kk = k > 0 ? k : 1;
+    const int64_t chunk = std::max<int64_t>(32, std::min<int64_t>(L, (int64_t(256) << 20) / (sizeof(T) * kk)));
+    void* tmp = nullptr;
+    if (cudaMallocAsync(&tmp, sizeof(T) * kk * chunk, stream) != cudaSuccess) return;
+    for (int64_t r0 = 0; r0 < L; r0 += chunk) {
+        const int64_t rows = std::min(chunk, L - r0);
+        if (k > 0) {
+            dim3 grid(static_cast<unsigned>((rows + 31) / 32), static_cast<unsigned>((k + 31) / 32));
+            rotate_chunk_kernel<T><<<grid, 256, 0, stream>>>(Q, r0, rows, ldq, w, R, ldr, k, static_cast<T*>(tmp));
+            count_launch();
+        }
+        rotate_chunk_store_kernel<T, O><<<grid_for(rows * (k + 1), 256, 152 * 16), 256, 0, stream>>>(
+            static_cast<const T*>(tmp), r0, rows, k, out, ldo, fcol, fnorm);
+        count_launch();
+    }
+    cudaFreeAsync(tmp, stream);
+}
+
 template <typename T, typename O>
 void rotate_dispatch(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, O* out,
                      int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream) {
+    if (w > 128) {
+        // Wide bases skip the abort check: the engine only rotates after a
+        // restart whose control block it has read (abort clear).
+        rotate_wide<T, O>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, stream);
+        return;
+    }
     if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value) {
         const bool aligned = ldq % 4 == 0 && ldo % 4 == 0 && reinterpret_cast<uintptr_t>(Q) % 16 == 0 &&
                              reinterpret_cast<uintptr_t>(out) % 16 == 0;

@@ -106,6 +106,12 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
  * host), or on the host (on = 0). Both give the same layout. */
 void irlba_gb300_set_device_ingest(int32_t on);
 
+/* Launch shape of the sparse products of FP32-form matrices created after
+ * this call: 0 = 256-thread CTAs; 1 = 256 threads, six CTAs per SM; 2 (the
+ * default) = 512 threads, three CTAs per SM. A tuning switch: results agree to
+ * rounding. */
+void irlba_gb300_set_spmv_shape(int32_t shape);
+
 /* Copies between pageable host memory and the device of at least `min_bytes`
  * (default 16 MiB; < 0: never) run through pinned staging buffers of
  * `slice_bytes` each (default 8 MiB; <= 0 keeps the current size), filled and

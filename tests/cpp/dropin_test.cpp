@@ -192,6 +192,10 @@ int main() {
     std::printf("\"chain_changed_iterations\": %d,\n", res3b.iterations);
     dump_vec("center_changed", center.data(), nc);
     dump_vec("scale_changed", scale.data(), nc);
+    for (std::ptrdiff_t c = 0; c < nc; ++c) {   // back to the vectors dumped above
+        center[c] = 0.01 * c;
+        scale[c] = 1.0 + 0.02 * c;
+    }
 
     // Dense input held with an outer stride (the top-left 100 x 50 block of A).
     StridedView view{A.data(), 100, 50, nr};

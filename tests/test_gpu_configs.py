@@ -59,8 +59,11 @@ def test_planted_dense_1000x200_k5(engine, oracle_mod):
         assert same_same(tight.D[j], S[j], 1e-6)
     assert np.max(column_sines(tight.U, U[:, :5])) < 1e-6
     assert np.max(column_sines(tight.V, Vt[:5].T)) < 1e-6
-    # The planted spectrum is recovered: 100, 90, 80, 70, 60 plus the noise bulk.
-    assert np.all(np.abs(gpu.D - np.array([100, 90, 80, 70, 60])) < 5)
+    # The planted directions dominate: the top five singular values are the
+    # planted 100, 90, ..., 60 lifted by the noise (about sqrt(s^2 + 1200)),
+    # well above the noise bulk (about sqrt(1000) + sqrt(200) = 45.8).
+    lifted = np.sqrt(np.array([100.0, 90, 80, 70, 60]) ** 2 + 1200)
+    assert np.all(np.abs(gpu.D - lifted) < 3) and gpu.D[-1] > 50
 
 
 def test_scrna_20k_x_50k_fp64_pca_full_size(engine, oracle_mod):

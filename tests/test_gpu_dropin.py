@@ -53,14 +53,14 @@ def test_dropin_decorated_sparse(dropin_output, oracle_mod):
     # The centre and scale vectors changed after the decorators were built:
     # the next compute uses the new contents (the reference reads them through
     # its pointers, centered.hpp:46-52, scaled.hpp:52-69). The workspace
-    # multiply below ran after the change as well.
+    # multiply below ran after the vectors were restored.
     spec2 = oracle_mod.Spec.sparse(nr, nc, x, i, p, True, 1, center=np.array(d["center_changed"]),
                                    scale=np.array(d["scale_changed"]))
     orc2 = oracle_mod.compute(spec2, 4, oracle_mod.options(initial=init))
     np.testing.assert_allclose(d["chain_changed_D"], orc2["D"], rtol=1e-10)
     assert d["chain_changed_iterations"] == orc2["iterations"]
     assert np.max(np.abs(np.array(d["chain_changed_D"]) - orc["D"]) / orc["D"]) > 1e-3
-    np.testing.assert_allclose(d["chain_multiply_init"], oracle_mod.multiply(spec2, init), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(d["chain_multiply_init"], oracle_mod.multiply(spec, init), rtol=1e-12, atol=1e-12)
     assert "cannot be greater than" in d["error_message"]
 
 
