@@ -1376,6 +1376,131 @@ static std::pair<bool, int> pca_device_impl(const irlba_gb300_matrix* matrix, in
 
 }  // namespace irlba_gb300
 
+namespace irlba_gb300 {
+
+// ---------------------------------------------------------------------------
+// Decorator chains beyond one centre and one scale (e.g. CenteredMatrix over
+// ScaledMatrix over CenteredMatrix, or row and column scaling together): the
+// chain runs as a device operator. Each product applies the decorators from
+// the outside in, as the reference's nested workspaces do
+// (centered.hpp:46-52,83-87; scaled.hpp:52-69,106-123):
+//   multiply  Centered: beta = c . x, y = inner(x) - beta
+//             Scaled column: y = inner(x * s or x / s)
+//             Scaled row: y = inner(x), then y * s or y / s
+//   adjoint   Centered: beta = sum x, y = inner^T(x) - beta c
+//             Scaled column: y = inner^T(x), then y * s or y / s
+//             Scaled row: y = inner^T(x * s or x / s)
+// with the base's own products at the bottom. The extra passes are over
+// vectors (length nrow or ncol), not over the matrix.
+// ---------------------------------------------------------------------------
+struct ChainOperator {
+    const BaseMatrix* base = nullptr;
+    std::vector<const irlba_gb300_matrix*> decos;
+    bool f64 = true;
+    std::vector<DevBuf> vecs;      // each decorator's vector in the form's type
+    std::vector<DevBuf> tmps;      // one scratch vector per decorator level
+    DevBuf betas, part, partial, ctrl_buf;
+    int64_t nrow = 0, ncol = 0;
+
+    template <typename T>
+    void base_product(bool adjoint, const T* x, T* y, cudaStream_t s) {
+        const Ctrl* ctrl = ctrl_buf.as<Ctrl>();
+        if (base->is_operator()) {
+            operator_product<T>(*base, adjoint, x, y, s);
+            return;
+        }
+        const DirPlan& p = adjoint ? base->adj : base->mul;
+        Epilogue<T> e;
+        launch_spmv<T>(p.dev, x, y, partial.as<T>(), e, &ctrl->abort, s);
+    }
+
+    template <typename T>
+    void apply(size_t level, bool adjoint, const T* x, T* y, cudaStream_t s) {
+        if (level == decos.size()) {
+            base_product<T>(adjoint, x, y, s);
+            return;
+        }
+        Ctrl* ctrl = ctrl_buf.as<Ctrl>();
+        const irlba_gb300_matrix* d = decos[level];
+        const T* v = vecs[level].as<T>();
+        T* tmp = tmps[level].as<T>();
+        double* beta = betas.as<double>() + level;
+        const int64_t lin = adjoint ? nrow : ncol, lout = adjoint ? ncol : nrow;
+        Epilogue<T> e;
+        if (d->kind == 1) {
+            // Centering: beta from the input, then one rank-1 correction.
+            launch_beta<T>(x, lin, nullptr, 0, adjoint ? nullptr : v, beta, part.as<double>(), ctrl, s);
+            apply<T>(level + 1, adjoint, x, y, s);
+            e.beta = beta;
+            if (adjoint) e.cvec = v;
+            launch_epilogue<T>(y, lout, e, &ctrl->abort, s);
+        } else if (static_cast<bool>(d->column) != adjoint) {
+            // Scaling on the input side (column scale of a multiply, row scale of an adjoint).
+            launch_scale_vector<T>(x, v, d->divide, lin, tmp, s);
+            apply<T>(level + 1, adjoint, tmp, y, s);
+        } else {
+            // Scaling on the output side.
+            apply<T>(level + 1, adjoint, x, y, s);
+            e.oscale = v;
+            e.odivide = d->divide;
+            launch_epilogue<T>(y, lout, e, &ctrl->abort, s);
+        }
+    }
+
+    static int32_t product(void* user, int32_t adjoint, const void* x, void* y, void* stream) {
+        auto* op = static_cast<ChainOperator*>(user);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        try {
+            if (op->f64) op->apply<double>(0, adjoint != 0, static_cast<const double*>(x), static_cast<double*>(y), s);
+            else op->apply<float>(0, adjoint != 0, static_cast<const float*>(x), static_cast<float*>(y), s);
+            return cudaGetLastError() == cudaSuccess ? 0 : 1;
+        } catch (const std::exception&) {
+            return 1;
+        }
+    }
+};
+
+std::shared_ptr<BaseMatrix> make_chain_operator(const BaseMatrix* base,
+                                                const std::vector<const irlba_gb300_matrix*>& decos) {
+    auto op = std::make_shared<ChainOperator>();
+    op->base = base;
+    op->decos = decos;
+    op->f64 = base->form == IRLBA_GB300_FORM_FP64;
+    op->nrow = base->nrow;
+    op->ncol = base->ncol;
+    const size_t tsz = op->f64 ? sizeof(double) : sizeof(float);
+    const int64_t lmax = std::max<int64_t>(std::max(base->nrow, base->ncol), 1);
+    for (const irlba_gb300_matrix* d : decos) {
+        if (op->f64) {
+            op->vecs.push_back(upload(d->vec.data(), d->vec.size()));
+        } else {
+            std::vector<float> f(d->vec.begin(), d->vec.end());
+            op->vecs.push_back(upload(f.data(), f.size()));
+        }
+        op->tmps.emplace_back(tsz * lmax);
+    }
+    op->betas.alloc(sizeof(double) * std::max<size_t>(decos.size(), 1));
+    op->part.alloc(sizeof(double) * (cgs_update_grid(lmax) + 64));
+    int64_t pmax = 1;
+    if (!base->is_operator())
+        pmax = std::max<int64_t>({pmax, base->mul.dev.npanels > 1 ? base->mul.dev.npanels * base->nrow : 0,
+                                  base->adj.dev.npanels > 1 ? base->adj.dev.npanels * base->ncol : 0});
+    op->partial.alloc(tsz * pmax);
+    op->ctrl_buf.alloc(sizeof(Ctrl));
+    CUDA_TRY(cudaMemset(op->ctrl_buf.ptr, 0, sizeof(Ctrl)));
+    auto bm = std::make_shared<BaseMatrix>();
+    bm->nrow = base->nrow;
+    bm->ncol = base->ncol;
+    bm->form = base->form;
+    bm->store_f64 = base->store_f64;
+    bm->op.device = &ChainOperator::product;
+    bm->op.user = op.get();
+    // The BaseMatrix keeps the operator alive through its deleter.
+    return std::shared_ptr<BaseMatrix>(bm.get(), [bm, op](BaseMatrix*) {});
+}
+
+}  // namespace irlba_gb300
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

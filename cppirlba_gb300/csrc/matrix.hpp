@@ -56,7 +56,14 @@ struct Chain {
     const std::vector<double>* scale = nullptr;
     int scale_column = 1, scale_divide = 1;
     int center_outer = 0;
+    std::shared_ptr<BaseMatrix> owned;  // the chain operator below, when one was built
 };
+
+// A decorator chain the fused kernels do not cover (more than one
+// CenteredMatrix or ScaledMatrix over the base, in any order) as a device
+// operator whose products walk the chain (engine.cu); decos[0] is outermost.
+std::shared_ptr<BaseMatrix> make_chain_operator(const BaseMatrix* base,
+                                                const std::vector<const irlba_gb300_matrix*>& decos);
 
 inline Chain flatten(const irlba_gb300_matrix* m) {
     std::vector<const irlba_gb300_matrix*> decos;
@@ -70,9 +77,11 @@ inline Chain flatten(const irlba_gb300_matrix* m) {
     ch.base = cur->base.get();
     int ncenter = 0, nscale = 0;
     for (auto* d : decos) (d->kind == 1 ? ncenter : nscale)++;
-    if (ncenter > 1 || nscale > 1)
-        throw Error(IRLBA_GB300_ERROR_UNSUPPORTED,
-                    "the GPU engine fuses at most one CenteredMatrix and one ScaledMatrix over a base matrix");
+    if (ncenter > 1 || nscale > 1) {
+        ch.owned = make_chain_operator(ch.base, decos);
+        ch.base = ch.owned.get();
+        return ch;
+    }
     for (auto* d : decos) {
         if (d->kind == 1) ch.center = &d->vec;
         else {

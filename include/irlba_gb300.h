@@ -36,7 +36,7 @@ typedef enum {
     IRLBA_GB300_ERROR_INVALID_ARGUMENT = 1, /* messages as the reference's std::runtime_error */
     IRLBA_GB300_ERROR_CUDA = 2,             /* a CUDA call failed (no GPU, out of memory, ...) */
     IRLBA_GB300_ERROR_NUMERICAL = 3,        /* e.g. starting vector near the null space */
-    IRLBA_GB300_ERROR_UNSUPPORTED = 4       /* a decorator chain the engine does not fuse */
+    IRLBA_GB300_ERROR_UNSUPPORTED = 4       /* e.g. a gradient through an unfused decorator chain */
 } irlba_gb300_status;
 
 typedef enum {

@@ -106,13 +106,17 @@ def test_decorator_chains(engine, oracle_mod, kind, chain):
     np.testing.assert_allclose(m.realize(), oracle_mod.realize(spec), rtol=1e-14, atol=1e-14)
 
 
-def test_unsupported_chain_is_an_error(engine):
+def test_double_centering_chain(engine):
+    # A CenteredMatrix over a CenteredMatrix (the reference's decorators nest
+    # freely) runs as a chain operator: M = I - 1 c1^T - 1 c2^T.
     base = engine.SimpleMatrix(np.eye(6))
-    c1 = engine.CenteredMatrix(base, np.ones(6))
-    c2 = engine.CenteredMatrix(c1, np.ones(6))
-    with pytest.raises(engine.IrlbaError) as e:
-        c2.multiply(np.ones(6))
-    assert e.value.status == engine.ERROR_UNSUPPORTED
+    c1, c2 = np.arange(6.0), np.ones(6)
+    m = engine.CenteredMatrix(engine.CenteredMatrix(base, c1), c2)
+    M = np.eye(6) - c1[None, :] - c2[None, :]
+    v = np.linspace(-1, 2, 6)
+    np.testing.assert_allclose(m.multiply(v), M @ v, rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(m.adjoint_multiply(v), M.T @ v, rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(m.realize(), M, rtol=1e-13, atol=1e-13)
 
 
 def test_fp32_form_matvec(engine, oracle_mod):
