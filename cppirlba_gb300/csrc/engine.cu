@@ -61,6 +61,7 @@ DeviceInfo& device_info() {
         CUDA_TRY(spmv_configure(kPanelBytes));
         TRACE("device_info: rotate attributes");
         CUDA_TRY(rotate_configure(sizeof(double) * 128 * 128));
+        CUDA_TRY(rotate_tc_configure(info.max_smem_optin));
         TRACE("device_info: restart attributes");
         CUDA_TRY(restart_configure(info.max_smem_optin));
         TRACE("device_info: batch attributes");
@@ -166,6 +167,25 @@ static int plan_shape(bool staged, bool store_f64, bool x_f64) {
     return (staged && !store_f64 && !x_f64) ? g_spmv_shape : 0;
 }
 
+// Lanes per segment of the gather from the average segment length in 16-byte
+// vectors. With FP64 vectors (FP64 accumulation) the per-segment FP64 work
+// (combining a lane's partial sums, the shuffle tree, the epilogue) costs as
+// much as the products on GB300's narrow FP64 pipe unless several segments
+// share each warp instruction, so those groups stay at 4 lanes, or 8 for
+// segments of 256 vectors and more (measured: 100-vector cell rows 4 lanes
+// 13 % faster than 8, 800-vector gene panel segments 8 lanes 11 % faster
+// than 4). FP32 groups take 32 lanes only for long segments (several
+// hundred vectors); below that, 8 lanes and four segments per warp keep more
+// loads in flight between the per-segment reductions (measured on the
+// 2,000-gene single-cell matrices: 50 vectors per cell row, 8 lanes 10 %
+// faster than 16; about 400 per gene panel segment, 32 lanes fastest).
+static int plan_group_lanes(int64_t nnz, int64_t nseg, bool store_f64, bool x_f64) {
+    const double avg = nseg > 0 ? static_cast<double>(nnz) / static_cast<double>(nseg) : 0.0;
+    const double vecs = avg / (store_f64 ? 2.0 : 4.0);
+    if (x_f64) return vecs >= 256 ? 8 : 4;
+    return vecs >= 128 ? 32 : vecs >= 6 ? 8 : 4;
+}
+
 static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirPlan& plan) {
     TRACE("build_plan: %lld x %lld, nnz %lld", (long long)h.rows, (long long)h.cols, (long long)h.ptr[h.rows]);
     const DeviceInfo& di = device_info();
@@ -243,12 +263,7 @@ static void build_plan(const HostCompressed& h, bool store_f64, bool x_f64, DirP
     // Balance CTAs over segments by cost = nnz + kSegCost per segment.
     d.smem_bytes = staged ? static_cast<size_t>(d.panel_width) * xbytes : 0;
     TRACE("build_plan: occupancy query");
-    // Lanes per segment from the average segment length (in 16-byte vectors).
-    {
-        const double avg = nseg > 0 ? static_cast<double>(nnz) / static_cast<double>(nseg) : 0.0;
-        const double vecs = avg / (store_f64 ? 2.0 : 4.0);
-        d.group_lanes = vecs >= 96 ? 32 : vecs >= 24 ? 16 : vecs >= 6 ? 8 : 4;
-    }
+    d.group_lanes = plan_group_lanes(nnz, nseg, store_f64, x_f64);
     d.shape = plan_shape(staged, store_f64, x_f64);
     const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes, d.group_lanes, d.shape);
     TRACE("build_plan: %d blocks per SM", per_sm);
@@ -339,11 +354,7 @@ static void build_plan_device(const DevCompressed& h, bool store_f64, bool x_f64
         CUDA_TRY(cudaStreamSynchronize(s));
     }
     d.smem_bytes = staged ? static_cast<size_t>(d.panel_width) * xbytes : 0;
-    {
-        const double avg = nseg > 0 ? static_cast<double>(nnz) / static_cast<double>(nseg) : 0.0;
-        const double vecs = avg / (store_f64 ? 2.0 : 4.0);
-        d.group_lanes = vecs >= 96 ? 32 : vecs >= 24 ? 16 : vecs >= 6 ? 8 : 4;
-    }
+    d.group_lanes = plan_group_lanes(nnz, nseg, store_f64, x_f64);
     d.shape = plan_shape(staged, store_f64, x_f64);
     const int per_sm = spmv_blocks_per_sm(staged, store_f64, x_f64, d.smem_bytes, d.group_lanes, d.shape);
     int64_t nblocks = static_cast<int64_t>(di.sms) * per_sm;
@@ -948,6 +959,8 @@ struct Engine {
         CUDA_TRY(cudaEventRecord(ev1, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         CUDA_TRY(cudaGetLastError());
+        if (std::is_same<T, float>::value && rotate_tc_take_error() != 0)
+            throw Error(IRLBA_GB300_ERROR_CUDA, "a tensor-core basis rotation timed out on a wait");
         float dev_ms = 0;
         cudaEventElapsedTime(&dev_ms, ev0, ev1);
         cudaEventDestroy(ev0);

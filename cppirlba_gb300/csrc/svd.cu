@@ -286,39 +286,47 @@ __global__ void __cluster_dims__(kClusterCTAs, 1, 1) __launch_bounds__(kClusterT
 //     -theta_pq), X <- X (I + D) with
 //       D = -E/2 + K + 3/8 E^2 + 1/2 K^2 - 1/2 E K,
 //     the second-order expansion of (I - E/2 + 3/8 E^2)(I + K + 1/2 K^2).
-//     C and N are formed in FP64; D and the product X D only need FP32
-//     (their rounding is below what the next step removes), so each step's
-//     error falls by a factor of about 1e-7 or quadratically in the
+//     C and N are formed in FP64; D, the angles and the product X D only need
+//     FP32 (their rounding is below what the next step removes), so each
+//     step's error falls by a factor of about 1e-7 or quadratically in the
 //     off-diagonal size, whichever is smaller. Pairs with |theta| > 1e-4
 //     (singular values too close for the FP32 stage to separate) are left out
-//     of K and rotated exactly instead: c = cos theta, s = sin theta in FP64,
-//     applied one after the other after the matrix update. It stops when
-//     every pair has |C_pq| <= 8 eps sqrt(C_pp C_qq) and |N_pq - delta_pq| <=
-//     8 eps, or, once both are below n eps (the skip threshold of the
-//     one-sided Jacobi above), when a step no longer shrinks the coupling 4x
-//     (the rounding floor of the Gram sums); columns of a null G are exempt
-//     from the first test. This is a mixed-precision Jacobi method in the
-//     sense of Higham, Tisseur, Webb and Zhou (refinement of a low-precision
-//     Jacobi SVD in higher precision), here with the refinement written as
-//     matrix products instead of sweeps.
+//     of K and rotated exactly instead, after the matrix update, in a fixed
+//     order (column q, then row p); their cosines and sines are FP32 values
+//     scaled to c^2 + s^2 = 1 in FP64, so the rotations are orthogonal to FP64
+//     precision. It stops when every pair has |C_pq| <= 8 eps sqrt(C_pp C_qq)
+//     and |N_pq - delta_pq| <= 8 eps, or, once both are below n eps (the skip
+//     threshold of the one-sided Jacobi above), when a step no longer shrinks
+//     the coupling 4x (the rounding floor of the Gram sums); columns of a null
+//     G are exempt from the first test. This is a mixed-precision Jacobi method
+//     in the sense of Higham, Tisseur, Webb and Zhou (refinement of a
+//     low-precision Jacobi SVD in higher precision), here with the refinement
+//     written as matrix products instead of sweeps.
 //  3. If the refinement has not converged after kRefMaxSteps steps, CTA 0
 //     runs the FP64 one-sided Jacobi above on B itself.
-// The cluster's CTAs all run step 1 on the same data (identical results, no
-// broadcast); in step 2 CTA r forms the Gram entries (p <= q) of the columns
-// q = r, r + R, ... and the new columns X[:, q], and every CTA copies its
-// results into the others' shared memory before a cluster barrier.
-// Singular values are then the norms of G = B X, as in the Jacobi form
-// (finish_svd: sort, U = G / sigma, completion for zero singular values,
-// canonical signs).
+// Work split: the cluster's CTAs all run step 1 on the same data (identical
+// results, no broadcast). In step 2 CTA r owns the columns q = r, r + R, ...:
+// it forms G[:, q] = B X[:, q], C_qq and the FP32 copy of X[:, q], then the
+// Gram entries (p <= q) and the new X[:, q], and copies each result into
+// every CTA's shared memory before the cluster barrier that publishes it
+// (three per step). Every CTA applies the exact rotations to its own full
+// copy of X, in the same order (thread i rotates row i, so no barrier
+// separates them). Singular values are then the norms of G = B X, as in the
+// Jacobi form; each CTA writes the singular values and the U = G / sigma and
+// V = X columns of its own columns in sorted order with canonical signs (the
+// finish_svd conventions), and CTA 0 runs the restart tail. If a singular
+// value is zero (U has to be completed) CTA 0 finishes alone with finish_svd.
 // ---------------------------------------------------------------------------
 constexpr int kRefCTAs = 8;
 constexpr int kRefThreads = 512;
 constexpr int kRefMaxN = 64;
-constexpr int kRefLd = 65;          // column stride of the shared-memory matrices (odd: fewer bank conflicts)
+constexpr int kRefLd = 65;          // column stride of the FP64 matrices (odd: fewer bank conflicts)
+constexpr int kJ32Ld = 64;          // column stride of the FP32 Jacobi matrices (rows n..63 zero)
 constexpr int kRefMaxSteps = 8;
 constexpr int kRefMaxSweeps32 = 30;
 constexpr float kRefTol32 = 1e-6f;
-constexpr float kRefBigAngle = 1e-4f;   // |theta| above this: an exact FP64 rotation
+constexpr float kRefStop32 = 1e-4f;     // a sweep whose rotations all had |cos| below this is the last
+constexpr float kRefBigAngle = 1e-4f;   // |theta| above this: an exact rotation
 constexpr int kRefMaxBig = 256;         // exact rotations per step (the rest wait a step)
 constexpr int kRefOwn = (kRefMaxN + kRefCTAs - 1) / kRefCTAs;   // columns owned per CTA
 
@@ -329,137 +337,239 @@ struct RefSmem {
     double E[kRefMaxN * kRefLd];     // N - I, upper triangle (q >= p at [q * ld + p])
     union {
         struct {                     // step 1
-            float G32[kRefMaxN * kRefLd];
-            float V32[kRefMaxN * kRefLd];
+            float4 G32[kRefMaxN * kJ32Ld / 4];
+            float4 V32[kRefMaxN * kJ32Ld / 4];
+            unsigned short ptab[kRefMaxN * 32];   // round r, slot s: p | q << 8 (p < q), 0xffff: no pair
         } s1;
         struct {                     // step 2
-            float K32[kRefMaxN * kRefLd];   // theta_pq, upper triangle
-            float E32[kRefMaxN * kRefLd];   // E, both triangles
+            float2 EK[kRefMaxN * kRefLd];   // (E_pq, theta_pq) at [q * ld + p]: upper triangle, then full
             float D32[kRefOwn * kRefLd];    // D[:, own columns]
             float X32[kRefMaxN * kRefLd];
         } s2;
     } u;
-    double lam[kRefMaxN];            // diag(C)
-    double rsq[kRefMaxN];            // 1 / sqrt(C_pp), 0 for null columns
-    double maxima[2 * kRefCTAs];     // per CTA: max relative off-diagonal of C, max |E|
+    double lam[kRefMaxN];            // C_jj = |G[:, j]|^2
+    float lamf[kRefMaxN];            // C_jj / max C
+    float rsqf[kRefMaxN];            // (C_jj / max C)^(-1/2), 0 for null columns
+    double inv_lmax;
+    float maxima[2 * kRefCTAs];      // per CTA: max relative off-diagonal of C, max |E|
+    float redf[64];
     double big_c[kRefMaxBig], big_s[kRefMaxBig];
     unsigned char big_p[kRefMaxBig], big_q[kRefMaxBig];
+    int big_cnt[kRefMaxN];           // large angles in column q, then their offsets
     int nbig;
     int nzc[kRefMaxN][4];            // nonzero columns of each row of B (count in nzn)
     int nzn[kRefMaxN];
     double norms[kRefMaxN];
     int order[kRefMaxN];
+    int rankof[kRefMaxN];
+    double invsg[kRefMaxN];          // canonical sign / singular value of column j (from its owner)
+    double prevS[kRefMaxN];          // the previous restart's singular values
+    double tail_res[kRefMaxN];
+    double R_F;
+    int tail_conv, tail_kn;
     double pairs[3 * kRefMaxN];
     double red[32];
+    unsigned long long redu[32];
     int rotated, sweeps, notconv;
+    unsigned int j32max;
 };
 
-// One-sided Jacobi in FP32 on G (n x n, column stride kRefLd) accumulating V,
-// rotating a pair when |g_p . g_q| > tol |g_p| |g_q|. Eight lanes per pair
-// (four pairs per warp), lane l of a pair holding rows l, l + 8, ..., so a
-// round costs three shuffle levels per sum; rotation parameters by every lane
-// of the pair (Rutishauser's formulas). n <= 64. Returns the sweeps made.
-constexpr int kJ32Lanes = 8;
-constexpr int kJ32Rows = kRefMaxN / kJ32Lanes;
-__device__ int jacobi32_sweeps(float* G, float* V, int n, float tol) {
+// One-sided Jacobi in FP32 on G (n x n) accumulating V, both stored as n
+// columns of kJ32Ld floats (rows n..63 zero), rotating a pair when
+// (g_p . g_q)^2 > tol^2 |g_p|^2 |g_q|^2. Sixteen lanes per pair (two pairs per
+// warp, so 16 warps cover the 32 slots of n <= 64), lane l holding rows
+// 4l .. 4l + 3 of both columns of G and V in one 16-byte load each, so a
+// round is four loads, a four-level shuffle tree, the rotation and one CTA
+// barrier. The pairs of each round come from ptab (the circle ordering,
+// prepared once); the rotation is Rutishauser's, written as
+// t = sign(d) 2 g / (|d| + sqrt(d^2 + 4 g^2)), d = |g_q|^2 - |g_p|^2, with the
+// hardware reciprocal and reciprocal square root: this stage only has to
+// bring the angles below what the FP64 refinement resolves. The sweeps stop
+// when a sweep rotates nothing, or when the largest |cos| it rotated was
+// below `stop` (the next sweep would take them to about stop^2: no further
+// sweep is needed for the refinement). jmax: one shared word, zero on entry.
+// The rounds are limited by shared-memory and shuffle throughput (every
+// column is read each round), so V is read only for pairs that rotate.
+// Returns the sweeps made.
+__device__ int jacobi32_sweeps(float4* G, float4* V, const unsigned short* ptab, int n, float tol, float stop,
+                               unsigned int* jmax) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nw = static_cast<int>(blockDim.x >> 5);
-    const int sub = lane / kJ32Lanes, gl = lane % kJ32Lanes;
+    const int sub = lane >> 4, gl = lane & 15;
     const int n2 = n + (n & 1), half = n2 / 2;
+    const int nrounds = n2 - 1;
+    const int slot = 2 * warp + sub;
+    const bool busy = 2 * warp < half;     // warp-uniform
+    const float tol2 = tol * tol, stop2 = stop * stop;
+    constexpr int kC = kJ32Ld / 4;         // float4 per column
     int sweep = 0;
     for (; sweep < kRefMaxSweeps32; ++sweep) {
         int rotated = 0;
-        for (int round = 0; round < n2 - 1; ++round) {
-            for (int slot = warp * (32 / kJ32Lanes) + sub; slot - sub < half; slot += nw * (32 / kJ32Lanes)) {
-                int p = 0, q = n;
-                if (slot < half) {
-                    p = circle_partner_a(round, slot, n2);
-                    q = circle_partner_b(round, slot, n2);
-                    if (p > q) {
-                        const int tmp = p;
-                        p = q;
-                        q = tmp;
-                    }
+        float cmax2 = 0.f;
+        unsigned int pq_next = (busy && slot < half) ? ptab[slot] : 0xffffu;
+        for (int round = 0; round < nrounds; ++round) {
+            const unsigned int pq = pq_next;
+            if (busy && slot < half && round + 1 < nrounds) pq_next = ptab[(round + 1) * 32 + slot];
+            if (busy) {
+                const bool live = pq != 0xffffu;
+                const int p = static_cast<int>(pq & 0xffu), q = static_cast<int>(pq >> 8);
+                float4 x = make_float4(0.f, 0.f, 0.f, 0.f), y = x;
+                if (live) {
+                    x = G[p * kC + gl];
+                    y = G[q * kC + gl];
                 }
-                const bool live = q < n;
-                float* gp = G + p * kRefLd;
-                float* gq = G + q * kRefLd;
-                float x[kJ32Rows], y[kJ32Rows];
-                float a = 0.f, b = 0.f, g = 0.f;
+                float a = x.x * x.x, b = y.x * y.x, g = x.x * y.x;
+                a = fmaf(x.y, x.y, a);
+                b = fmaf(y.y, y.y, b);
+                g = fmaf(x.y, y.y, g);
+                a = fmaf(x.z, x.z, a);
+                b = fmaf(y.z, y.z, b);
+                g = fmaf(x.z, y.z, g);
+                a = fmaf(x.w, x.w, a);
+                b = fmaf(y.w, y.w, b);
+                g = fmaf(x.w, y.w, g);
 #pragma unroll
-                for (int t = 0; t < kJ32Rows; ++t) {
-                    const int i = gl + t * kJ32Lanes;
-                    x[t] = (live && i < n) ? gp[i] : 0.f;
-                    y[t] = (live && i < n) ? gq[i] : 0.f;
-                    a = fmaf(x[t], x[t], a);
-                    b = fmaf(y[t], y[t], b);
-                    g = fmaf(x[t], y[t], g);
-                }
-#pragma unroll
-                for (int o = kJ32Lanes / 2; o > 0; o >>= 1) {
+                for (int o = 8; o > 0; o >>= 1) {
                     a += __shfl_xor_sync(0xffffffffu, a, o);
                     b += __shfl_xor_sync(0xffffffffu, b, o);
                     g += __shfl_xor_sync(0xffffffffu, g, o);
                 }
-                if (live && fabsf(g) > tol * sqrtf(a) * sqrtf(b)) {
-                    const float zeta = (b - a) / (2.f * g);
-                    const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-                    const float c = rsqrtf(1.f + tt * tt), sn = c * tt;
-                    float* vp = V + p * kRefLd;
-                    float* vq = V + q * kRefLd;
-#pragma unroll
-                    for (int t = 0; t < kJ32Rows; ++t) {
-                        const int i = gl + t * kJ32Lanes;
-                        if (i < n) {
-                            gp[i] = c * x[t] - sn * y[t];
-                            gq[i] = sn * x[t] + c * y[t];
-                            const float u = vp[i], v = vq[i];
-                            vp[i] = c * u - sn * v;
-                            vq[i] = sn * u + c * v;
-                        }
-                    }
+                if (live && g * g > tol2 * a * b) {
+                    const float4 u = V[p * kC + gl], v = V[q * kC + gl];
+                    cmax2 = fmaxf(cmax2, __fdividef(g * g, a * b));
+                    const float d = b - a;
+                    const float h = fmaf(d, d, 4.f * g * g);
+                    const float den = fabsf(d) + h * rsqrtf(h);
+                    const float t = __fdividef((d >= 0.f ? 2.f : -2.f) * g, den);
+                    const float c = rsqrtf(fmaf(t, t, 1.f)), s = c * t;
+                    G[p * kC + gl] = make_float4(c * x.x - s * y.x, c * x.y - s * y.y, c * x.z - s * y.z,
+                                                 c * x.w - s * y.w);
+                    G[q * kC + gl] = make_float4(s * x.x + c * y.x, s * x.y + c * y.y, s * x.z + c * y.z,
+                                                 s * x.w + c * y.w);
+                    V[p * kC + gl] = make_float4(c * u.x - s * v.x, c * u.y - s * v.y, c * u.z - s * v.z,
+                                                 c * u.w - s * v.w);
+                    V[q * kC + gl] = make_float4(s * u.x + c * v.x, s * u.y + c * v.y, s * u.z + c * v.z,
+                                                 s * u.w + c * v.w);
                     rotated = 1;
                 }
             }
             __syncthreads();
         }
-        if (!__syncthreads_or(rotated)) break;
+        const unsigned int wm = __reduce_max_sync(0xffffffffu, __float_as_uint(cmax2));
+        if ((threadIdx.x & 31) == 0 && wm != 0u) atomicMax(jmax, wm);
+        __syncthreads();
+        const float m2 = __uint_as_float(*jmax);
+        const int go_on = __syncthreads_or(rotated) && !(m2 < stop2);
+        if (threadIdx.x == 0) *jmax = 0u;
+        if (!go_on) break;
     }
     return sweep + 1;
 }
 
-// G = B X with B's rows given as lists of nonzero columns (rows with more than
-// four nonzeros are marked with nzn = -1 and summed densely).
-__device__ void ref_bx(RefSmem& S, int n) {
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int j = e / n, i = e % n;
-        const double* x = S.X + j * kRefLd;
-        double acc = 0;
-        const int cnt = S.nzn[i];
-        if (cnt >= 0) {
-            for (int t = 0; t < cnt; ++t) {
-                const int l = S.nzc[i][t];
-                acc += S.B[l * kRefLd + i] * x[l];
-            }
-        } else {
-            for (int l = i; l < n; ++l) acc += S.B[l * kRefLd + i] * x[l];
-        }
-        S.G[j * kRefLd + i] = acc;
+// Maxima of two non-negative values over the CTA, valid in every thread. red:
+// 64 floats not otherwise in use until the CTA's next barrier after this call.
+__device__ void ref_block_max2f(float& x, float& y, float* red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
+        y = fmaxf(y, __shfl_xor_sync(0xffffffffu, y, o));
+    }
+    if (lane == 0) {
+        red[warp] = x;
+        red[32 + warp] = y;
+    }
+    __syncthreads();
+    x = 0.f;
+    y = 0.f;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+        x = fmaxf(x, red[w]);
+        y = fmaxf(y, red[32 + w]);
     }
 }
 
-// Maximum of v over the CTA (fixed order), valid in every thread.
-__device__ double ref_block_max(double v, double* red) {
+// Maximum of v over the CTA, valid in every thread (integer: the order of
+// non-negative doubles is the order of their bit patterns).
+__device__ unsigned long long ref_block_maxu(unsigned long long v, unsigned long long* red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
     if (lane == 0) red[warp] = v;
     __syncthreads();
-    double m = 0;
-    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
-    __syncthreads();
+    unsigned long long m = 0;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) m = red[w] > m ? red[w] : m;
     return m;
+}
+
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7fffffffffffffffull;
+}
+
+// The restart tail of restart_tail (the convergence test, update_k and the
+// rebuild of B, with the same predicates and values) on CTA 0 of the refine
+// kernel, from shared memory: the singular values and their order, B, and the
+// sign / singular value factors the owners of the columns used, so that
+// U[last, jj] = G[last, j] * invsg[j] is the value the owner wrote.
+__device__ void refine_tail(const RestartArgs& a, RefSmem& S, int sweeps) {
+    Ctrl* ctrl = a.ctrl;
+    const int n = a.work;
+    const int last = n - 1;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        int converged = 0;
+        int n_conv = 0;
+        if (S.B[last * kRefLd + last] == 0.0) {
+            converged = 1;
+        } else {
+            const double R_F = S.R_F;
+            for (int jj = lane; jj < n; jj += 32) {
+                const int j = S.order[jj];
+                const double r = R_F * (S.G[j * kRefLd + last] * S.invsg[j]);
+                S.tail_res[jj] = r;
+                a.res[jj] = r;
+            }
+        }
+        if (!converged && a.iter > 0) {
+            const double threshold = S.norms[S.order[0]] * a.tol;
+            int cnt = 0;
+            for (int jj = lane; jj < n; jj += 32) {
+                if (fabs(S.tail_res[jj]) <= threshold) {
+                    const double bs = S.norms[S.order[jj]];
+                    const double ratio = fabs(bs - S.prevS[jj]) / bs;
+                    if (ratio <= a.svtol) ++cnt;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            n_conv = cnt;
+            if (n_conv >= a.requested) converged = 1;
+        }
+        if (!converged)
+            for (int jj = lane; jj < n; jj += 32) a.prevS[jj] = S.norms[S.order[jj]];
+        if (lane == 0) {
+            const int kn = converged ? a.k : update_k_dev(a.k, a.requested, n_conv, n);
+            ctrl->svd_sweeps = sweeps;
+            ctrl->svd_not_converged = 0;
+            ctrl->converged = converged;
+            ctrl->n_converged = n_conv;
+            ctrl->k_next = kn;
+            S.tail_conv = converged;
+            S.tail_kn = kn;
+        }
+    }
+    __syncthreads();
+    if (!S.tail_conv) {
+        const int kn = S.tail_kn;
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+            const int j = e / n, i = e % n;
+            double v = 0.0;
+            if (i < kn && j == i) v = S.norms[S.order[i]];
+            else if (i < kn && j == kn) v = S.tail_res[i];
+            a.B[e] = v;
+        }
+    }
 }
 
 __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
@@ -474,39 +584,69 @@ __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
     const int rank = static_cast<int>(cl.block_rank());
     const int n = a.work;
     const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nw = static_cast<int>(blockDim.x >> 5);
 
-    // B into shared memory, its row structure, and the FP32 copy scaled by max |B|.
-    double bmax = 0;
+    // B into shared memory, its row structure, and the FP32 copy scaled by max
+    // |B| (the comparisons on integer bit patterns: FP64 compares use the
+    // narrow FP64 pipe); the pair table of the FP32 Jacobi; the previous
+    // singular values and ||F|| for the tail.
+    unsigned long long bmaxu = 0;
     for (int e = tid; e < n * n; e += blockDim.x) {
         const int j = e / n, i = e % n;
         const double v = a.B[static_cast<int64_t>(j) * n + i];
         S.B[j * kRefLd + i] = v;
-        bmax = fmax(bmax, fabs(v));
+        const unsigned long long av = abs_bits(v);
+        bmaxu = av > bmaxu ? av : bmaxu;
     }
-    bmax = ref_block_max(bmax, S.red);
+    if (rank == 0) {
+        for (int j = tid; j < n; j += blockDim.x) S.prevS[j] = a.prevS[j];
+        if (tid == 0) S.R_F = a.ctrl->norm_F;
+    }
+    if (tid == 0) S.j32max = 0u;
+    {
+        const int n2 = n + (n & 1), half = n2 / 2;
+        for (int e = tid; e < (n2 - 1) * 32; e += blockDim.x) {
+            const int round = e / 32, slot = e % 32;
+            unsigned short v = 0xffffu;
+            if (slot < half) {
+                int p = circle_partner_a(round, slot, n2), q = circle_partner_b(round, slot, n2);
+                if (p > q) {
+                    const int tmp = p;
+                    p = q;
+                    q = tmp;
+                }
+                if (q < n) v = static_cast<unsigned short>(p | (q << 8));
+            }
+            S.u.s1.ptab[e] = v;
+        }
+    }
+    const double bmax = __longlong_as_double(static_cast<long long>(ref_block_maxu(bmaxu, S.redu)));
     const float inv = bmax > 0 ? static_cast<float>(1.0 / bmax) : 1.f;
     for (int i = tid; i < n; i += blockDim.x) {
         int cnt = 0;
         for (int l = 0; l < n; ++l) {
-            if (S.B[l * kRefLd + i] != 0.0) {
+            if (abs_bits(S.B[l * kRefLd + i]) != 0ull) {
                 if (cnt < 4) S.nzc[i][cnt] = l;
                 ++cnt;
             }
         }
         S.nzn[i] = cnt <= 4 ? cnt : -1;
     }
-    for (int e = tid; e < n * n; e += blockDim.x) {
-        const int j = e / n, i = e % n;
-        S.u.s1.G32[j * kRefLd + i] = static_cast<float>(S.B[j * kRefLd + i]) * inv;
-        S.u.s1.V32[j * kRefLd + i] = (i == j) ? 1.f : 0.f;
+    float* G32 = reinterpret_cast<float*>(S.u.s1.G32);
+    float* V32 = reinterpret_cast<float*>(S.u.s1.V32);
+    for (int e = tid; e < n * kJ32Ld; e += blockDim.x) {
+        const int j = e / kJ32Ld, i = e % kJ32Ld;
+        G32[e] = i < n ? static_cast<float>(S.B[j * kRefLd + i]) * inv : 0.f;
+        V32[e] = i == j ? 1.f : 0.f;
     }
     __syncthreads();
 
     // Step 1: FP32 Jacobi (every CTA, identical results).
-    jacobi32_sweeps(S.u.s1.G32, S.u.s1.V32, n, kRefTol32);
+    jacobi32_sweeps(S.u.s1.G32, S.u.s1.V32, S.u.s1.ptab, n, kRefTol32, kRefStop32, &S.j32max);
     for (int e = tid; e < n * n; e += blockDim.x) {
         const int j = e / n, i = e % n;
-        S.X[j * kRefLd + i] = static_cast<double>(S.u.s1.V32[j * kRefLd + i]);
+        S.X[j * kRefLd + i] = static_cast<double>(V32[j * kJ32Ld + i]);
     }
     // The FP32 arrays share storage with what the other CTAs write next.
     cl.sync();
@@ -522,39 +662,64 @@ __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
         ++nown;
     }
     const int nitems = own_off[nown];
-    const double eps = 2.220446049250313e-16;
+    const float feps = 2.220446049250313e-16f;
+    float2* EK = S.u.s2.EK;
 
     int steps = 0;
     bool converged = false;
-    double prev_off = 1.0;
+    float prev_off = 1.f;
     for (; steps <= kRefMaxSteps; ++steps) {
-        // X is stable until this step's update phase (the other CTAs write
-        // their new columns only after the barrier below).
-        ref_bx(S, n);
-        for (int e = tid; e < n * n; e += blockDim.x) {
-            const int j = e / n, i = e % n;
-            S.u.s2.X32[j * kRefLd + i] = static_cast<float>(S.X[j * kRefLd + i]);
+        // (a) G[:, q] = B X[:, q], C_qq and the FP32 copy of X[:, q] for the own
+        // columns (one warp per column), into every CTA.
+        if (warp < nown) {
+            const int q = own_q[warp];
+            const double* x = S.X + q * kRefLd;
+            double ss = 0;
+            for (int i = lane; i < n; i += 32) {
+                double acc = 0;
+                const int cnt = S.nzn[i];
+                if (cnt >= 0) {
+                    for (int t = 0; t < cnt; ++t) {
+                        const int l = S.nzc[i][t];
+                        acc += S.B[l * kRefLd + i] * x[l];
+                    }
+                } else {
+                    for (int l = i; l < n; ++l) acc += S.B[l * kRefLd + i] * x[l];
+                }
+                ss += acc * acc;
+                const float x32 = static_cast<float>(x[i]);
+                for (int r = 0; r < kRefCTAs; ++r) {
+                    cl.map_shared_rank(S.G, r)[q * kRefLd + i] = acc;
+                    cl.map_shared_rank(S.u.s2.X32, r)[q * kRefLd + i] = x32;
+                }
+            }
+            ss = warp_sum(ss);
+            if (lane < kRefCTAs) cl.map_shared_rank(S.lam, lane)[q] = ss;
         }
-        __syncthreads();
-        // diag(C) and 1 / sqrt(C_pp) (0 for columns of a null G).
-        double lmax = 0;
-        for (int j = tid; j < n; j += blockDim.x) {
-            const double* g = S.G + j * kRefLd;
-            double s = 0;
-            for (int i = 0; i < n; ++i) s += g[i] * g[i];
-            S.lam[j] = s;
-            lmax = fmax(lmax, s);
+        cl.sync();
+        // C_jj / max C in FP32 for the angles and the coupling measure.
+        if (warp == 0) {
+            const double l0 = lane < n ? S.lam[lane] : 0.0, l1 = lane + 32 < n ? S.lam[lane + 32] : 0.0;
+            double lm = fmax(l0, l1);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+            const double il = lm > 0 ? 1.0 / lm : 0.0;
+            if (lane == 0) S.inv_lmax = il;
+            const float nfl = static_cast<float>(n) * feps;
+            for (int j = lane; j < n; j += 32) {
+                const float lf = static_cast<float>(S.lam[j] * il);
+                S.lamf[j] = lf;
+                S.rsqf[j] = lf > nfl * nfl ? rsqrtf(lf) : 0.f;
+            }
         }
-        lmax = ref_block_max(lmax, S.red);
-        const double null_floor = lmax * (eps * n) * (eps * n);
-        for (int j = tid; j < n; j += blockDim.x) S.rsq[j] = S.lam[j] > null_floor ? rsqrt(S.lam[j]) : 0.0;
         __syncthreads();
 
-        // Gram items of the own columns: C_pq, N_pq; E_pq and theta_pq to every
-        // CTA. Four lanes per item (rows i = l, l + 4, ...), so the FP64 work
-        // spreads over all warps of the CTA.
-        double offmax = 0, emax = 0;
+        // (b) Gram entries of the own columns: C_pq, N_pq in FP64, four lanes
+        // per entry (rows i = l, l + 4, ...), so the FP64 work spreads over all
+        // warps; E_pq and theta_pq to every CTA (each lane of the four writes two).
+        float offmax = 0.f, emax = 0.f;
         const int q4 = tid & 3;
+        const double il = S.inv_lmax;
         for (int it0 = 0; it0 < nitems; it0 += static_cast<int>(blockDim.x >> 2)) {
             const int it = it0 + (tid >> 2);
             const bool has = it < nitems;
@@ -576,136 +741,240 @@ __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
             nn += __shfl_xor_sync(0xffffffffu, nn, 1);
             c += __shfl_xor_sync(0xffffffffu, c, 2);
             nn += __shfl_xor_sync(0xffffffffu, nn, 2);
-            if (!has || q4 != 0) continue;
             const double e = nn - (p == q ? 1.0 : 0.0);
-            emax = fmax(emax, fabs(e));
             float th = 0.f;
-            if (p != q && c != 0.0) {
-                // tan 2 theta = 2 C_pq / (C_qq - C_pp), |theta| <= pi / 4, from
-                // the scaled C_pq sqrt(1 / (C_pp C_qq)) and difference (no FP64
-                // division on the common path).
-                const double rp = S.rsq[p], rq = S.rsq[q];
-                float num, den;
-                if (rp > 0 && rq > 0) {
-                    const double r = rp * rq;
-                    const double cr = c * r;
-                    offmax = fmax(offmax, fabs(cr));
-                    num = static_cast<float>(cr);
-                    den = static_cast<float>((S.lam[q] - S.lam[p]) * r);
-                } else if (rp > 0 || rq > 0) {
-                    // One column of a null G: a small rotation against the other.
-                    const double big = rp > 0 ? S.lam[p] : S.lam[q];
-                    num = static_cast<float>(c / big);
-                    den = rp > 0 ? -1.f : 1.f;
-                } else {
-                    num = 0.f;
-                    den = 1.f;
+            if (has && q4 == 0) {
+                emax = fmaxf(emax, fabsf(static_cast<float>(e)));
+                if (p != q && c != 0.0) {
+                    // tan 2 theta = 2 C_pq / (C_qq - C_pp), |theta| <= pi / 4, from
+                    // C scaled by its largest diagonal entry.
+                    const float rp = S.rsqf[p], rq = S.rsqf[q];
+                    const float cn = static_cast<float>(c * il);
+                    float num, den;
+                    if (rp > 0.f && rq > 0.f) {
+                        const float r = rp * rq;
+                        num = cn * r;
+                        offmax = fmaxf(offmax, fabsf(num));
+                        den = static_cast<float>((S.lam[q] - S.lam[p]) * il) * r;
+                    } else if (rp > 0.f || rq > 0.f) {
+                        // One column of a null G: a small rotation against the other.
+                        num = cn / (rp > 0.f ? S.lamf[p] : S.lamf[q]);
+                        den = rp > 0.f ? -1.f : 1.f;
+                    } else {
+                        num = 0.f;
+                        den = 1.f;
+                    }
+                    if (num != 0.f) th = den == 0.f ? copysignf(0.78539816f, num) : 0.5f * atanf(2.f * num / den);
                 }
-                if (num != 0.f) th = den == 0.f ? copysignf(0.78539816f, num) : 0.5f * atanf(2.f * num / den);
             }
-            for (int r = 0; r < kRefCTAs; ++r) {
-                double* Er = cl.map_shared_rank(S.E, r);
-                float* Kr = cl.map_shared_rank(S.u.s2.K32, r);
-                Er[q * kRefLd + p] = e;
-                Kr[q * kRefLd + p] = th;
+            th = __shfl_sync(0xffffffffu, th, lane & ~3);
+            if (has) {
+                const float2 ek = make_float2(static_cast<float>(e), th);
+                for (int r = q4; r < kRefCTAs; r += 4) {
+                    cl.map_shared_rank(S.E, r)[q * kRefLd + p] = e;
+                    cl.map_shared_rank(EK, r)[q * kRefLd + p] = ek;
+                }
             }
         }
-        offmax = ref_block_max(offmax, S.red);
-        emax = ref_block_max(emax, S.red);
-        if (tid == 0)
-            for (int r = 0; r < kRefCTAs; ++r) {
-                double* mr = cl.map_shared_rank(S.maxima, r);
-                mr[2 * rank] = offmax;
-                mr[2 * rank + 1] = emax;
-            }
+        ref_block_max2f(offmax, emax, S.redf);
+        if (tid < kRefCTAs) {
+            float* mr = cl.map_shared_rank(S.maxima, tid);
+            mr[2 * rank] = offmax;
+            mr[2 * rank + 1] = emax;
+        }
         cl.sync();
-        double goff = 0, gem = 0;
+        float goff = 0.f, gem = 0.f;
         for (int r = 0; r < kRefCTAs; ++r) {
-            goff = fmax(goff, S.maxima[2 * r]);
-            gem = fmax(gem, S.maxima[2 * r + 1]);
+            goff = fmaxf(goff, S.maxima[2 * r]);
+            gem = fmaxf(gem, S.maxima[2 * r + 1]);
         }
         // Converged at 8 eps; or, once below the one-sided Jacobi's skip
         // threshold n eps, as soon as a step no longer shrinks the coupling by
         // 4x (the Gram sums' rounding floor).
-        if ((goff <= 8 * eps && gem <= 8 * eps) ||
-            (goff <= n * eps && gem <= n * eps && goff > 0.25 * prev_off)) {
+        const float nf = static_cast<float>(n);
+        if ((goff <= 8.f * feps && gem <= 8.f * feps) ||
+            (goff <= nf * feps && gem <= nf * feps && goff > 0.25f * prev_off)) {
             converged = true;
             break;
         }
         prev_off = goff;
         if (steps == kRefMaxSteps) break;
 
-        // D[:, own] = -E/2 + K + 3/8 E^2 + 1/2 K^2 - 1/2 E K (second order in FP32).
-        for (int e = tid; e < n * n; e += blockDim.x) {
-            const int q = e / n, p = e % n;
-            S.u.s2.E32[q * kRefLd + p] = static_cast<float>(p <= q ? S.E[q * kRefLd + p] : S.E[p * kRefLd + q]);
+        // (c) The large angles in a fixed order (column q, then row p): counts
+        // per column, their offsets, then the entries (one warp per column).
+        for (int q = warp; q < n; q += nw) {
+            int cnt = 0;
+            for (int p0 = 0; p0 < q; p0 += 32) {
+                const int p = p0 + lane;
+                cnt += __popc(__ballot_sync(0xffffffffu, p < q && fabsf(EK[q * kRefLd + p].y) > kRefBigAngle));
+            }
+            if (lane == 0) S.big_cnt[q] = cnt;
         }
         __syncthreads();
-        auto Eat = [&](int p, int q) -> float { return S.u.s2.E32[q * kRefLd + p]; };
-        auto Kat = [&](int p, int q) -> float {
-            const float t = p == q ? 0.f : (p < q ? S.u.s2.K32[q * kRefLd + p] : -S.u.s2.K32[p * kRefLd + q]);
-            return fabsf(t) > kRefBigAngle ? 0.f : t;
-        };
-        // The large angles, in a fixed order (column q, then row p), with
-        // their FP64 cosines and sines.
-        if (tid < 32) {
-            int count = 0;
-            for (int q = 1; q < n; ++q) {
-                for (int p0 = 0; p0 < q; p0 += 32) {
-                    const int p = p0 + tid;
-                    const bool big = p < q && fabsf(S.u.s2.K32[q * kRefLd + p]) > kRefBigAngle;
-                    const unsigned m = __ballot_sync(0xffffffffu, big);
-                    const int slot = count + __popc(m & ((1u << tid) - 1u));
-                    if (big && slot < kRefMaxBig) {
-                        S.big_p[slot] = static_cast<unsigned char>(p);
-                        S.big_q[slot] = static_cast<unsigned char>(q);
-                    }
-                    count += __popc(m);
+        if (warp == 0) {
+            const int c0 = lane < n ? S.big_cnt[lane] : 0;
+            const int c1 = lane + 32 < n ? S.big_cnt[lane + 32] : 0;
+            int s0 = c0, s1 = c1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t0 = __shfl_up_sync(0xffffffffu, s0, o), t1 = __shfl_up_sync(0xffffffffu, s1, o);
+                if (lane >= o) {
+                    s0 += t0;
+                    s1 += t1;
                 }
             }
-            if (tid == 0) S.nbig = count < kRefMaxBig ? count : kRefMaxBig;
+            const int tot0 = __shfl_sync(0xffffffffu, s0, 31), tot1 = __shfl_sync(0xffffffffu, s1, 31);
+            __syncwarp();
+            if (lane < n) S.big_cnt[lane] = s0 - c0;
+            if (lane + 32 < n) S.big_cnt[lane + 32] = tot0 + s1 - c1;
+            if (lane == 0) S.nbig = tot0 + tot1 < kRefMaxBig ? tot0 + tot1 : kRefMaxBig;
         }
         __syncthreads();
-        for (int b = tid; b < S.nbig; b += blockDim.x) {
-            const double t = static_cast<double>(S.u.s2.K32[S.big_q[b] * kRefLd + S.big_p[b]]);
-            sincos(t, &S.big_s[b], &S.big_c[b]);
+        for (int q = warp; q < n; q += nw) {
+            int base = S.big_cnt[q];
+            for (int p0 = 0; p0 < q; p0 += 32) {
+                const int p = p0 + lane;
+                const bool big = p < q && fabsf(EK[q * kRefLd + p].y) > kRefBigAngle;
+                const unsigned m = __ballot_sync(0xffffffffu, big);
+                const int slot = base + __popc(m & ((1u << lane) - 1u));
+                if (big && slot < kRefMaxBig) {
+                    S.big_p[slot] = static_cast<unsigned char>(p);
+                    S.big_q[slot] = static_cast<unsigned char>(q);
+                }
+                base += __popc(m);
+            }
         }
+        __syncthreads();
+        const int nbig = S.nbig;
+        // Cosines and sines of the large angles: FP32 sincos, then scaled to
+        // c^2 + s^2 = 1 in FP64 ((1 + d)^(-1/2) to second order in d ~ 1e-7).
+        for (int b = tid; b < nbig; b += blockDim.x) {
+            float s32, c32;
+            sincosf(EK[S.big_q[b] * kRefLd + S.big_p[b]].y, &s32, &c32);
+            const double c = c32, s = s32;
+            const double d = fma(c, c, fma(s, s, -1.0));
+            const double f = fma(0.375 * d, d, fma(-0.5, d, 1.0));
+            S.big_c[b] = c * f;
+            S.big_s[b] = s * f;
+        }
+        __syncthreads();
+        // The full E (symmetric) and K (skew, large angles removed) in FP32:
+        // each thread completes one pair (p < q) or a diagonal entry.
+        for (int e = tid; e < n * (n + 1) / 2; e += blockDim.x) {
+            // e -> (p, q) with p <= q, column by column.
+            int q = static_cast<int>((sqrtf(8.f * e + 1.f) - 1.f) * 0.5f);
+            while (q * (q + 1) / 2 > e) --q;
+            while ((q + 1) * (q + 2) / 2 <= e) ++q;
+            const int p = e - q * (q + 1) / 2;
+            float2 v = EK[q * kRefLd + p];
+            if (p == q || fabsf(v.y) > kRefBigAngle) v.y = 0.f;
+            EK[q * kRefLd + p] = v;
+            if (p != q) EK[p * kRefLd + q] = make_float2(v.x, -v.y);
+        }
+        __syncthreads();
+
+        // (d) D[:, own] = -E/2 + K + 3/8 E^2 + 1/2 K^2 - 1/2 E K (second order in
+        // FP32), then X[:, q] += X D[:, q] for the own columns, into every CTA.
         for (int e = tid; e < nown * n; e += blockDim.x) {
             const int o = e / n, p = e % n, q = own_q[o];
             float ee = 0, kk = 0, ek = 0;
             for (int r = 0; r < n; ++r) {
-                const float epr = Eat(p, r), kpr = Kat(p, r);
-                const float erq = Eat(r, q), krq = Kat(r, q);
-                ee += epr * erq;
-                kk += kpr * krq;
-                ek += epr * krq;
+                const float2 pr = EK[r * kRefLd + p], rq = EK[q * kRefLd + r];
+                ee = fmaf(pr.x, rq.x, ee);
+                kk = fmaf(pr.y, rq.y, kk);
+                ek = fmaf(pr.x, rq.y, ek);
             }
             const double first = -0.5 * (p <= q ? S.E[q * kRefLd + p] : S.E[p * kRefLd + q]) +
-                                 static_cast<double>(Kat(p, q));
+                                 static_cast<double>(EK[q * kRefLd + p].y);
             S.u.s2.D32[o * kRefLd + p] = static_cast<float>(first) + (0.375f * ee + 0.5f * kk - 0.5f * ek);
         }
         __syncthreads();
-        // X[:, q] += X D[:, q] for the own columns, into every CTA.
         for (int e = tid; e < nown * n; e += blockDim.x) {
             const int o = e / n, i = e % n, q = own_q[o];
             float acc = 0;
             const float* d = S.u.s2.D32 + o * kRefLd;
-            for (int p = 0; p < n; ++p) acc += S.u.s2.X32[p * kRefLd + i] * d[p];
+            for (int p = 0; p < n; ++p) acc = fmaf(S.u.s2.X32[p * kRefLd + i], d[p], acc);
             const double xn = S.X[q * kRefLd + i] + static_cast<double>(acc);
             for (int r = 0; r < kRefCTAs; ++r) cl.map_shared_rank(S.X, r)[q * kRefLd + i] = xn;
         }
         cl.sync();
-        // The exact rotations, on every CTA's copy of X (same order, same result):
-        // x_p <- c x_p - s x_q, x_q <- s x_p + c x_q.
-        for (int b = 0; b < S.nbig; ++b) {
-            const int p = S.big_p[b], q = S.big_q[b];
-            const double c = S.big_c[b], sn = S.big_s[b];
-            for (int i = tid; i < n; i += blockDim.x) {
-                const double xv = S.X[p * kRefLd + i], yv = S.X[q * kRefLd + i];
-                S.X[p * kRefLd + i] = c * xv - sn * yv;
-                S.X[q * kRefLd + i] = sn * xv + c * yv;
+        // (e) The exact rotations on this CTA's full copy of X: thread i rotates
+        // row i through the whole list (x_p <- c x_p - s x_q, x_q <- s x_p + c x_q).
+        if (tid < n) {
+            for (int b = 0; b < nbig; ++b) {
+                const int p = S.big_p[b], q = S.big_q[b];
+                const double c = S.big_c[b], sn = S.big_s[b];
+                const double xv = S.X[p * kRefLd + tid], yv = S.X[q * kRefLd + tid];
+                S.X[p * kRefLd + tid] = c * xv - sn * yv;
+                S.X[q * kRefLd + tid] = sn * xv + c * yv;
             }
-            __syncthreads();
+        }
+        __syncthreads();
+    }
+
+    if (converged) {
+        // Singular values |G[:, j]| = sqrt(C_jj), their reciprocals and their
+        // order (every CTA; the order compares bit patterns, ties by index).
+        for (int j = tid; j < n; j += blockDim.x) {
+            const double sj = sqrt(S.lam[j]);
+            S.norms[j] = sj;
+            S.pairs[j] = 1.0 / sj;
+        }
+        __syncthreads();
+        for (int j = tid; j < n; j += blockDim.x) {
+            const long long sj = __double_as_longlong(S.norms[j]);
+            int r = 0;
+            for (int i = 0; i < n; ++i) {
+                const long long si = __double_as_longlong(S.norms[i]);
+                if (si > sj || (si == sj && i < j)) ++r;
+            }
+            S.order[r] = j;
+            S.rankof[j] = r;
+        }
+        __syncthreads();
+        const double zero_tol = S.norms[S.order[0]] * 2.220446049250313e-16 * static_cast<double>(n);
+        if (S.norms[S.order[n - 1]] > zero_tol) {
+            // The own columns: V = X, U = G / sigma, the largest-magnitude entry
+            // of each V column (first on ties) made positive.
+            if (warp < nown) {
+                const int j = own_q[warp], jj = S.rankof[j];
+                const double* x = S.X + j * kRefLd;
+                unsigned long long best = 0;
+                int arg = n;
+                for (int i = lane; i < n; i += 32) {
+                    const unsigned long long av = abs_bits(x[i]);
+                    if (arg == n || av > best) {
+                        best = av;
+                        arg = i;
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+                    if (oa < n && (arg == n || ob > best || (ob == best && oa < arg))) {
+                        best = ob;
+                        arg = oa;
+                    }
+                }
+                const bool neg = arg < n && x[arg] < 0.0;
+                const double sj = S.norms[j];
+                const double invs = neg ? -S.pairs[j] : S.pairs[j];
+                if (lane == 0) {
+                    a.BS[jj] = sj;
+                    cl.map_shared_rank(S.invsg, 0)[j] = invs;
+                }
+                for (int i = lane; i < n; i += 32) {
+                    a.BV[static_cast<int64_t>(jj) * n + i] = neg ? -x[i] : x[i];
+                    a.BU[static_cast<int64_t>(jj) * n + i] = S.G[j * kRefLd + i] * invs;
+                }
+            }
+            // Every CTA's columns are in global memory, and their factors in
+            // CTA 0, before CTA 0's tail.
+            cl.sync();
+            if (rank != 0) return;
+            refine_tail(a, S, steps);
+            return;
         }
     }
     // No CTA touches another's shared memory after this barrier.

@@ -99,6 +99,48 @@ __global__ void __launch_bounds__(kThreads) cgs_dot_kernel(const T* __restrict__
     }
 }
 
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    typedef float4 V;
+    static constexpr int N = 4;
+};
+template <>
+struct Vec16<double> {
+    typedef double2 V;
+    static constexpr int N = 2;
+};
+
+template <typename T>
+__device__ __forceinline__ void vec16_fma(T* s, const float4& x, T tj) {
+    s[0] += x.x * tj;
+    s[1] += x.y * tj;
+    s[2] += x.z * tj;
+    s[3] += x.w * tj;
+}
+template <typename T>
+__device__ __forceinline__ void vec16_fma(T* s, const double2& x, T tj) {
+    s[0] += x.x * tj;
+    s[1] += x.y * tj;
+}
+__device__ __forceinline__ double vec16_update(float4& x, const float* s) {
+    x.x -= s[0];
+    x.y -= s[1];
+    x.z -= s[2];
+    x.w -= s[3];
+    double q = static_cast<double>(x.x) * static_cast<double>(x.x);
+    q += static_cast<double>(x.y) * static_cast<double>(x.y);
+    q += static_cast<double>(x.z) * static_cast<double>(x.z);
+    q += static_cast<double>(x.w) * static_cast<double>(x.w);
+    return q;
+}
+__device__ __forceinline__ double vec16_update(double2& x, const double* s) {
+    x.x -= s[0];
+    x.y -= s[1];
+    return x.x * x.x + x.y * x.y;
+}
+
 // Sum of count partials by the whole CTA in a fixed order (thread-strided, then
 // the block tree); the result is valid in thread 0.
 __device__ __forceinline__ double reduce_partials(const double* part, int count, double* red) {
@@ -151,6 +193,80 @@ __global__ void __launch_bounds__(kThreads) cgs_update_kernel(const T* __restric
         const double s = reduce_partials(part, static_cast<int>(gridDim.x), red);
         if (threadIdx.x == 0) {
             const double nrm = sqrt(s);
+            *norm_out = nrm;
+            if (check_null && nrm < ctrl->eps) {
+                ctrl->null_start = 1;
+                ctrl->abort = 1;
+            } else if (check_eps && nrm < ctrl->eps) {
+                ctrl->invariant = 1;
+                ctrl->abort = 1;
+            }
+            ctrl->ticket[kTicketUpdate] = 0;
+        }
+    }
+}
+
+// The update pass with four FP32 or two FP64 consecutive rows per thread: one
+// 16-byte load per basis column and eight columns in flight, so a warp keeps
+// 4 KB of loads outstanding (the form above keeps 512 B, too few to cover
+// HBM latency at full bandwidth). Each row's products are summed in column
+// order exactly as above, so v is the same; only the norm's partial sums
+// group differently. Needs ldq a multiple of the row count and 16-byte
+// aligned Q and v; rows past the last full group are done by the first CTA.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cgs_update_vec_kernel(const T* __restrict__ Q, int64_t L, int64_t ldq,
+                                                                  int32_t c, const double* __restrict__ t,
+                                                                  T* __restrict__ v, double* __restrict__ part,
+                                                                  double* norm_out, int32_t check_eps,
+                                                                  int32_t check_null, Ctrl* ctrl) {
+    typedef typename Vec16<T>::V V;
+    constexpr int N = Vec16<T>::N;
+    __shared__ T ts[kMaxCols];
+    __shared__ double red[32];
+    __shared__ bool is_last;
+    if (ctrl->abort) return;
+    const int cs = c < kMaxCols ? c : kMaxCols;
+    for (int j = threadIdx.x; j < cs; j += blockDim.x) ts[j] = static_cast<T>(t[j]);
+    __syncthreads();
+
+    double sq = 0;
+    const int64_t nv = L / N;
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < nv;
+         g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = g * N;
+        T s[N];
+#pragma unroll
+        for (int u = 0; u < N; ++u) s[u] = 0;
+        const T* __restrict__ q = Q + r;
+        int j = 0;
+        for (; j + 7 < cs; j += 8) {
+            V x[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) x[u] = *reinterpret_cast<const V*>(q + (j + u) * ldq);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) vec16_fma<T>(s, x[u], ts[j + u]);
+        }
+        for (; j < cs; ++j) vec16_fma<T>(s, *reinterpret_cast<const V*>(q + j * ldq), ts[j]);
+        for (; j < c; ++j) vec16_fma<T>(s, *reinterpret_cast<const V*>(q + j * ldq), static_cast<T>(__ldg(t + j)));
+        V x = *reinterpret_cast<V*>(v + r);
+        sq += vec16_update(x, s);
+        *reinterpret_cast<V*>(v + r) = x;
+    }
+    if (blockIdx.x == 0)
+        for (int64_t r = nv * N + threadIdx.x; r < L; r += blockDim.x) {
+            T s = 0;
+            for (int j = 0; j < c; ++j) s += Q[r + j * ldq] * (j < cs ? ts[j] : static_cast<T>(__ldg(t + j)));
+            const T nvv = v[r] - s;
+            v[r] = nvv;
+            sq += static_cast<double>(nvv) * static_cast<double>(nvv);
+        }
+    const double bs = block_sum(sq, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = bs;
+
+    if (last_block(&ctrl->ticket[kTicketUpdate], &is_last)) {
+        const double tot = reduce_partials(part, static_cast<int>(gridDim.x), red);
+        if (threadIdx.x == 0) {
+            const double nrm = sqrt(tot);
             *norm_out = nrm;
             if (check_null && nrm < ctrl->eps) {
                 ctrl->null_start = 1;
@@ -374,6 +490,109 @@ __global__ void __launch_bounds__(256) rotate_f32_gemm_kernel(const float* Q, in
     }
 }
 
+// The same FP32 rotation with the Q tiles streamed through two shared-memory
+// buffers by cp.async (16-byte copies completing in the background), so the
+// next tile's loads overlap this tile's products, and with the column groups
+// at or past k idle (k = 50 of 64 leaves three of sixteen groups without
+// products). Needs ldq % 4 == 0 and a 16-byte aligned Q; the last, partial
+// tile is loaded with guarded plain loads. Every CTA reads all rows of a tile
+// into shared memory before it writes any output row of that tile, so out
+// may be Q itself.
+constexpr size_t kRotPipeSmem = sizeof(float) * (64 * 64 + 2 * 64 * kRotTileRows);
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+__global__ void __launch_bounds__(256) rotate_f32_pipe_kernel(const float* Q, int64_t L, int64_t ldq, int32_t w,
+                                                             const double* __restrict__ R, int32_t ldr, int32_t k,
+                                                             float* out, int64_t ldo, const float* __restrict__ fcol,
+                                                             const double* fnorm, const int32_t* abort) {
+    extern __shared__ __align__(16) float rsm[];
+    float* Rs = rsm;                // Rs[j * 64 + i]
+    float* Qb = rsm + 64 * 64;      // two tiles, Qb[buf][j * kRotTileRows + row]
+    if (abort && *abort) return;
+    const int64_t ntiles = (L + kRotTileRows - 1) / kRotTileRows;
+    auto issue = [&](int64_t tile, int buf) {
+        const int64_t r0 = tile * kRotTileRows;
+        float* dst = Qb + buf * (64 * kRotTileRows);
+        if (r0 + kRotTileRows <= L) {
+            for (int idx = threadIdx.x; idx < w * (kRotTileRows / 4); idx += blockDim.x) {
+                const int j = idx / (kRotTileRows / 4), q = idx % (kRotTileRows / 4);
+                cp_async16(dst + j * kRotTileRows + 4 * q, Q + r0 + 4 * q + j * ldq);
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < w * (kRotTileRows / 4); idx += blockDim.x) {
+                const int j = idx / (kRotTileRows / 4), q = idx % (kRotTileRows / 4);
+                const int64_t r = r0 + 4 * q;
+                *reinterpret_cast<float4*>(dst + j * kRotTileRows + 4 * q) = load4_guarded(Q + r + j * ldq, r, L);
+            }
+        }
+        cp_async_commit();
+    };
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles) issue(tile, 0);
+    for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
+        const int j = idx / 64, i = idx % 64;
+        Rs[idx] = (j < w && i < k) ? static_cast<float>(R[j + static_cast<int64_t>(i) * ldr]) : 0.0f;
+    }
+    const float finv = fcol ? static_cast<float>(1.0 / *fnorm) : 0.0f;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const bool cols = 4 * ty < k;
+    int buf = 0;
+    for (; tile < ntiles; tile += gridDim.x) {
+        const int64_t next = tile + gridDim.x;
+        if (next < ntiles) issue(next, buf ^ 1);
+        else cp_async_commit();
+        cp_async_wait_prev();
+        __syncthreads();
+        const float* Qs = Qb + buf * (64 * kRotTileRows);
+        const int64_t r0 = tile * kRotTileRows;
+        float acc[8][4];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
+        if (cols) {
+            for (int j = 0; j < w; ++j) {
+                const float4 q0 = *reinterpret_cast<const float4*>(Qs + j * kRotTileRows + 4 * tx);
+                const float4 q1 = *reinterpret_cast<const float4*>(Qs + j * kRotTileRows + 64 + 4 * tx);
+                const float4 rr = *reinterpret_cast<const float4*>(Rs + j * 64 + 4 * ty);
+                const float qa[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+                const float rb[4] = {rr.x, rr.y, rr.z, rr.w};
+#pragma unroll
+                for (int a = 0; a < 8; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(qa[a], rb[b], acc[a][b]);
+            }
+        }
+        if (fcol)
+            for (int idx = threadIdx.x; idx < kRotTileRows; idx += blockDim.x) {
+                const int64_t r = r0 + idx;
+                if (r < L) out[r + static_cast<int64_t>(k) * ldo] = fcol[r] * finv;
+            }
+        if (cols) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int col = 4 * ty + b;
+                if (col < k) {
+                    const int64_t ra = r0 + 4 * tx, rb2 = r0 + 64 + 4 * tx;
+                    store4_guarded(out + ra + col * ldo, ra, L, acc[0][b], acc[1][b], acc[2][b], acc[3][b]);
+                    store4_guarded(out + rb2 + col * ldo, rb2, L, acc[4][b], acc[5][b], acc[6][b], acc[7][b]);
+                }
+            }
+        }
+        // Every thread is done with this buffer before the next issue refills it.
+        __syncthreads();
+        buf ^= 1;
+    }
+    cp_async_wait_all();
+}
+
 // Rotations with more than 128 basis columns: tmp (rows x k, ld rows) =
 // Q[r0 : r0 + rows, :w] R[:w, :k] with 32 x 32 output tiles and 32-column
 // steps through w in shared memory; then tmp is copied over out (in place is
@@ -449,6 +668,8 @@ static void rotate_wide(const T* Q, int64_t L, int64_t ldq, int32_t w, const dou
     cudaFreeAsync(tmp, stream);
 }
 
+static bool g_rotate_pipe_ok = false;
+
 template <typename T, typename O>
 void rotate_dispatch(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, O* out,
                      int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream) {
@@ -463,9 +684,15 @@ void rotate_dispatch(const T* Q, int64_t L, int64_t ldq, int32_t w, const double
                              reinterpret_cast<uintptr_t>(out) % 16 == 0;
         if (w <= 64 && k <= 64 && aligned) {
             const int64_t tiles = (L + kRotTileRows - 1) / kRotTileRows;
-            const int grid = static_cast<int>(tiles < 152 * 4 ? (tiles < 1 ? 1 : tiles) : 152 * 4);
-            rotate_f32_gemm_kernel<<<grid, 256, kRotGemmSmem, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol,
-                                                                        fnorm, abort);
+            if (g_rotate_pipe_ok) {
+                const int grid = static_cast<int>(tiles < 152 * 2 ? (tiles < 1 ? 1 : tiles) : 152 * 2);
+                rotate_f32_pipe_kernel<<<grid, 256, kRotPipeSmem, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol,
+                                                                            fnorm, abort);
+            } else {
+                const int grid = static_cast<int>(tiles < 152 * 4 ? (tiles < 1 ? 1 : tiles) : 152 * 4);
+                rotate_f32_gemm_kernel<<<grid, 256, kRotGemmSmem, stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol,
+                                                                            fnorm, abort);
+            }
             count_launch();
             return;
         }
@@ -618,7 +845,8 @@ void launch_cgs_dot(const T* Q, int64_t L, int64_t ldq, int32_t c, const T* v, d
     if (c <= 0 || L == 0) return;
     const dim3 grid(static_cast<unsigned>(cgs_dot_ranges<T>(L, c)),
                     static_cast<unsigned>((c + kThreads / 32 - 1) / (kThreads / 32)));
-    cgs_dot_kernel<T><<<grid, kThreads, 0, stream>>>(Q, L, ldq, c, v, part, t, ctrl); count_launch();
+    cgs_dot_kernel<T><<<grid, kThreads, 0, stream>>>(Q, L, ldq, c, v, part, t, ctrl);
+    count_launch();
 }
 
 int cgs_update_grid(int64_t L) { return grid_for(L, kThreads, 152 * 8); }
@@ -630,8 +858,17 @@ int cgs_dot_grid(int64_t L) {
 template <typename T>
 void launch_cgs_update(const T* Q, int64_t L, int64_t ldq, int32_t c, const double* t, T* v, double* part,
                        double* norm_out, int32_t check_eps, int32_t check_null, Ctrl* ctrl, cudaStream_t stream) {
-    cgs_update_kernel<T><<<cgs_update_grid(L), kThreads, 0, stream>>>(Q, L, ldq, c, t, v, part, norm_out, check_eps,
-                                                                     check_null, ctrl); count_launch();
+    constexpr int N = Vec16<T>::N;
+    const bool vec = ldq % N == 0 && reinterpret_cast<uintptr_t>(Q) % 16 == 0 &&
+                     reinterpret_cast<uintptr_t>(v) % 16 == 0 && L >= N;
+    if (vec) {
+        cgs_update_vec_kernel<T><<<grid_for(L / N, kThreads, 152 * 8), kThreads, 0, stream>>>(
+            Q, L, ldq, c, t, v, part, norm_out, check_eps, check_null, ctrl);
+    } else {
+        cgs_update_kernel<T><<<cgs_update_grid(L), kThreads, 0, stream>>>(Q, L, ldq, c, t, v, part, norm_out,
+                                                                         check_eps, check_null, ctrl);
+    }
+    count_launch();
 }
 
 template <typename T>
@@ -677,6 +914,11 @@ cudaError_t rotate_configure_one(size_t max_smem) {
 
 cudaError_t rotate_configure(size_t max_smem) {
     cudaError_t e = rotate_configure_one<float, float>(max_smem);
+    if (e == cudaSuccess && max_smem >= kRotPipeSmem) {
+        e = cudaFuncSetAttribute(rotate_f32_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(kRotPipeSmem));
+        g_rotate_pipe_ok = e == cudaSuccess;
+    }
     if (e == cudaSuccess) e = rotate_configure_one<double, double>(max_smem);
     if (e == cudaSuccess) e = rotate_configure_one<float, double>(max_smem);
     return e;

@@ -87,6 +87,7 @@ def load():
     lib.oracle_choose_work.restype = i64
     lib.oracle_choose_work.argtypes = [i64, i32, i64]
     lib.oracle_svd.argtypes = [i64, i64, pd, pd, pd, pd]
+    lib.oracle_svd_square.argtypes = [i64, pd, pd, pd, pd]
     lib.oracle_fill_random_normals.argtypes = [pd, i64, ctypes.c_uint64]
     _lib = lib
     return lib
@@ -288,6 +289,18 @@ def svd(A):
     S = np.zeros(p)
     V = np.zeros((p, n))
     load().oracle_svd(m, n, _pd(A), _pd(U), _pd(S), _pd(V))
+    return U.T.copy(), S, V.T.copy()
+
+
+def svd_square(A):
+    """The restart loop's SVD of a square B (two-sided Jacobi, as Eigen::JacobiSVD)."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    n = A.shape[0]
+    assert A.shape == (n, n)
+    U = np.zeros((n, n))
+    S = np.zeros(n)
+    V = np.zeros((n, n))
+    load().oracle_svd_square(n, _pd(A), _pd(U), _pd(S), _pd(V))
     return U.T.copy(), S, V.T.copy()
 
 

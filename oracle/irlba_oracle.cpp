@@ -9,9 +9,14 @@
 // The reference cannot be built here: it needs Eigen 5.0.0, aarand, subpar and
 // sanisizer, none of which is available offline. Three pieces therefore differ
 // from the reference by construction and are restated from published methods:
-//   * Eigen::JacobiSVD (compute.hpp:27-28)  -> one-sided Jacobi SVD (Hestenes 1958;
-//     Demmel & Veselic 1992), columns sorted by decreasing singular value, with an
-//     orthonormal completion of U for zero singular values.
+//   * Eigen::JacobiSVD (compute.hpp:27-28) of the square B in the restart loop
+//     (compute.hpp:225) -> a restatement of Eigen's two-sided Jacobi SVD for real
+//     square input (the published Kogbetliantz / Brent-Luk-Van Loan scheme as
+//     Eigen 5.0.0 orders and terminates it; jacobi_svd_square below), so the
+//     restart SVD stops where the reference's does; for the exact SVD of a
+//     rectangular matrix (compute.hpp:30-46) -> one-sided Jacobi SVD (Hestenes
+//     1958; Demmel & Veselic 1992), columns sorted by decreasing singular value,
+//     with an orthonormal completion of U for zero singular values.
 //   * aarand::standard_normal (utils.hpp:27,34) -> Box-Muller on two 53-bit uniforms
 //     drawn from std::mt19937_64 (u = (x >> 11) * 2^-53, mapped to (0, 1]).
 //   * subpar::parallelize_simple (parallel.hpp:36) -> OpenMP parallel region with
@@ -535,6 +540,139 @@ void jacobi_svd_tall(Index m, Index n, const double* A, double* S, double* U, do
     }
 }
 
+// Canonical signs shared by both SVD forms: the largest-magnitude entry of each
+// V column (first one on ties) is made positive, and the U column follows.
+// Eigen's own signs follow from its rotation sequence; a fixed convention keeps
+// the oracle and the GPU engine comparable wherever outputs depend on the signs
+// of B's singular vectors (the max-iterations output of compute.hpp:268-305).
+// Flipping a (u, v) pair leaves the restart (compute.hpp:244-293) unchanged up
+// to the signs of the rotated basis columns.
+void canonical_signs(Index m, Index n, double* U, double* V) {
+    for (Index jj = 0; jj < n; ++jj) {
+        double* v = V + jj * n;
+        Index arg = 0;
+        for (Index i = 1; i < n; ++i)
+            if (std::abs(v[i]) > std::abs(v[arg])) arg = i;
+        if (v[arg] < 0) {
+            for (Index i = 0; i < n; ++i) v[i] = -v[i];
+            for (Index i = 0; i < m; ++i) U[jj * m + i] = -U[jj * m + i];
+        }
+    }
+}
+
+// Two-sided Jacobi SVD of a real square n x n matrix A (column-major): the
+// algorithm of Eigen::JacobiSVD (Eigen 5.0.0) for square input, restated.
+//  * A is divided by its largest |entry| (1 if zero); U = V = I.
+//  * Sweeps over p = 1..n-1, q = 0..p-1 until a sweep finds every |A_pq| and
+//    |A_qp| at most max(smallest normal, 2 eps d), d the largest |A_ii| seen
+//    (updated after each rotation).
+//  * Each such 2x2 block [a b; c d'] is made symmetric by a left rotation
+//    (t = a + d', e = c - b; if |e| is below the smallest normal the identity,
+//    else s1 = 1 / sqrt(1 + (t/e)^2), c1 = (t/e) s1), then diagonalized by the
+//    symmetric Jacobi rotation of [x y; y z] (tau = (x - z) / (2|y|),
+//    t = 1 / (tau +- sqrt(tau^2 + 1)) with the sign of tau, n = 1/sqrt(t^2 + 1),
+//    c = n, s = -sign(t) sign(y) |t| n); the left rotation applied to A is
+//    the product of the first with the transpose of the second.
+//  * Rotations (c, s) act on a pair (x, y) as x' = c x + s y, y' = -s x + c y:
+//    on rows p, q of A from the left; on columns of A and V from the right with
+//    (c, -s); on columns of U with the left rotation.
+//  * Singular values |A_ii| times the scale, U column negated where A_ii < 0,
+//    then ordered decreasingly by repeatedly taking the largest remaining value
+//    (first on ties) and swapping it, with its U and V columns, into place.
+// Outputs: S (n), U (n x n), V (n x n); canonical signs applied.
+void jacobi_svd_square(Index n, const double* Ain, double* S, double* U, double* V) {
+    const double eps = std::numeric_limits<double>::epsilon();
+    const double tiny = std::numeric_limits<double>::min();
+    const double precision = 2 * eps;
+    double scale = 0;
+    for (Index e = 0; e < n * n; ++e) scale = std::max(scale, std::abs(Ain[e]));
+    if (scale == 0) scale = 1;
+    std::vector<double> A(static_cast<size_t>(n * n));
+    for (Index e = 0; e < n * n; ++e) A[e] = Ain[e] / scale;
+    std::fill(U, U + n * n, 0.0);
+    std::fill(V, V + n * n, 0.0);
+    for (Index i = 0; i < n; ++i) U[i * n + i] = V[i * n + i] = 1.0;
+    auto a = [&](Index r, Index c) -> double& { return A[c * n + r]; };
+    // x' = c x + s y, y' = -s x + c y over `len` entries with strides.
+    auto rot = [](double* x, double* y, Index len, Index stride, double c, double s) {
+        for (Index i = 0; i < len; ++i) {
+            const double xi = x[i * stride], yi = y[i * stride];
+            x[i * stride] = c * xi + s * yi;
+            y[i * stride] = -s * xi + c * yi;
+        }
+    };
+    double maxdiag = 0;
+    for (Index i = 0; i < n; ++i) maxdiag = std::max(maxdiag, std::abs(a(i, i)));
+    bool finished = false;
+    while (!finished) {
+        finished = true;
+        for (Index p = 1; p < n; ++p) {
+            for (Index q = 0; q < p; ++q) {
+                const double threshold = std::max(tiny, precision * maxdiag);
+                if (!(std::abs(a(p, q)) > threshold || std::abs(a(q, p)) > threshold)) continue;
+                finished = false;
+                // 2x2 block of rows/columns (p, q): [m00 m01; m10 m11].
+                double m00 = a(p, p), m01 = a(p, q), m10 = a(q, p), m11 = a(q, q);
+                double c1 = 1, s1 = 0;
+                const double t = m00 + m11, d = m10 - m01;
+                if (!(std::abs(d) < tiny)) {
+                    const double u = t / d;
+                    const double tmp = std::sqrt(1 + u * u);
+                    s1 = 1 / tmp;
+                    c1 = u / tmp;
+                }
+                {   // the left rotation (c1, s1) on the block's rows
+                    const double r00 = c1 * m00 + s1 * m10, r01 = c1 * m01 + s1 * m11;
+                    const double r10 = -s1 * m00 + c1 * m10, r11 = -s1 * m01 + c1 * m11;
+                    m00 = r00;
+                    m01 = r01;
+                    m10 = r10;
+                    m11 = r11;
+                }
+                double cr = 1, sr = 0;   // the symmetric Jacobi rotation of [m00 m01; m01 m11]
+                const double deno = 2 * std::abs(m01);
+                if (!(deno < tiny)) {
+                    const double tau = (m00 - m11) / deno;
+                    const double w = std::sqrt(tau * tau + 1);
+                    const double tt = tau > 0 ? 1 / (tau + w) : 1 / (tau - w);
+                    const double sign_t = tt > 0 ? 1.0 : -1.0;
+                    const double nn = 1 / std::sqrt(tt * tt + 1);
+                    sr = -sign_t * (m01 / std::abs(m01)) * std::abs(tt) * nn;
+                    cr = nn;
+                }
+                // Left rotation of A: (c1, s1) times the transpose (cr, -sr).
+                const double cl = c1 * cr + s1 * sr, sl = s1 * cr - c1 * sr;
+                rot(&a(p, 0), &a(q, 0), n, n, cl, sl);          // rows p, q
+                rot(U + p * n, U + q * n, n, 1, cl, sl);         // columns of U
+                rot(&a(0, p), &a(0, q), n, 1, cr, -sr);         // columns of A
+                rot(V + p * n, V + q * n, n, 1, cr, -sr);        // columns of V
+                maxdiag = std::max(maxdiag, std::max(std::abs(a(p, p)), std::abs(a(q, q))));
+            }
+        }
+    }
+    for (Index i = 0; i < n; ++i) {
+        const double d = a(i, i);
+        S[i] = std::abs(d);
+        if (d < 0)
+            for (Index r = 0; r < n; ++r) U[i * n + r] = -U[i * n + r];
+    }
+    for (Index i = 0; i < n; ++i) S[i] *= scale;
+    for (Index i = 0; i < n; ++i) {
+        Index pos = i;
+        for (Index j = i + 1; j < n; ++j)
+            if (S[j] > S[pos]) pos = j;
+        if (S[pos] == 0) break;
+        if (pos != i) {
+            std::swap(S[i], S[pos]);
+            for (Index r = 0; r < n; ++r) {
+                std::swap(U[i * n + r], U[pos * n + r]);
+                std::swap(V[i * n + r], V[pos * n + r]);
+            }
+        }
+    }
+    canonical_signs(n, n, U, V);
+}
+
 // Thin SVD of any m x n matrix: U (m x p), S (p), V (n x p), p = min(m, n).
 void jacobi_svd(Index m, Index n, const double* A, std::vector<double>& S, Dense& U, Dense& V) {
     const Index p = std::min(m, n);
@@ -753,7 +891,10 @@ std::pair<bool, int> compute(const Matrix& mat, Index number, double* outU, doub
             stats->lanczos_steps += work - k;
         }
 
-        jacobi_svd(work, work, B.v.data(), BS, BU, BV);           // :225
+        BS.assign(work, 0.0);                                     // :225
+        BU = Dense(work, work);
+        BV = Dense(work, work);
+        jacobi_svd_square(work, B.v.data(), BS.data(), BU.v.data(), BV.v.data());
         if (B(work - 1, work - 1) == 0) {                         // :231-234
             converged = true;
             break;
@@ -1122,6 +1263,11 @@ void oracle_svd(int64_t m, int64_t n, const double* A, double* U, double* S, dou
     std::copy(SS.begin(), SS.end(), S);
     std::copy(UU.v.begin(), UU.v.end(), U);
     std::copy(VV.v.begin(), VV.v.end(), V);
+}
+
+// The restart SVD of a square matrix (the Eigen::JacobiSVD restatement): U, V n x n.
+void oracle_svd_square(int64_t n, const double* A, double* U, double* S, double* V) {
+    jacobi_svd_square(n, A, S, U, V);
 }
 
 void oracle_fill_random_normals(double* vec, int64_t n, uint64_t seed) {

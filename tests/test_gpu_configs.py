@@ -7,7 +7,8 @@
   reference's own tolerance ladder (tests/src/compute.cpp:15-31, :92-123).
 * Sparse 20,000 genes x 50,000 cells, ~5 % dense, FP64 values (CSC genes x
   cells, i.e. the cells x genes CSR pca input), centred and scaled pca k=50,
-  tol 1e-5: plain FP64 GPU against the FP64 oracle at full size.
+  tol 1e-5: plain FP64 GPU against the FP64 oracle at full size (singular
+  vectors compared as the test's docstring explains).
 * Sparse 2,000 genes x 200,000 cells, ~10 % dense, FP32 values (the 1.3M-cell
   headline matrix's shape, one sixth of its cells): the FP32+FP64-steps form
   against the FP64 oracle on the same (FP32-rounded) values, singular values
@@ -67,6 +68,17 @@ def test_planted_dense_1000x200_k5(engine, oracle_mod):
 
 
 def test_scrna_20k_x_50k_fp64_pca_full_size(engine, oracle_mod):
+    """759 restarts to tol 1e-5 with neighbouring singular values as close as
+    3.3e-5 relative. Two FP64 runs that differ only in rounding agree here in
+    the way perturbation theory predicts (Davis-Kahan / Wedin): the sine between
+    the two j-th singular vectors is about delta / gap_j, gap_j the relative gap
+    to the nearest neighbouring singular value, with delta about 5e-13 between
+    this engine and the oracle and 1e-13 between the oracle with the reference's
+    two-sided Jacobi restart SVD and the oracle with a one-sided one. The 1e-8
+    sine bound is therefore asserted on the principal angles between the
+    subspaces and on every column with gap_j >= 1e-4, and as delta = sine x gap
+    <= 1e-12 on every column (on the closer columns 1e-8 would need delta below
+    3.3e-13, the spread of equally valid FP64 restart SVDs)."""
     from cppirlba_gb300 import datagen
     inp = datagen.scrna_csc_20k()         # 20,000 genes x 50,000 cells, 5 %, FP64
     assert (inp.nrow, inp.ncol) == (50000, 20000) and inp.nnz > 45_000_000
@@ -79,8 +91,15 @@ def test_scrna_20k_x_50k_fp64_pca_full_size(engine, oracle_mod):
     assert gpu.iterations == orc["iterations"]
     # variances = D^2 / (m - 1): 2e-10 on variances is 1e-10 on D.
     np.testing.assert_allclose(gpu.variances, orc["variances"], rtol=2e-10, atol=0)
-    assert np.max(column_sines(gpu.rotation, orc["rotation"])) < 1e-8
-    assert np.max(column_sines(gpu.scores, orc["scores"])) < 1e-8
+    sv = np.sqrt(orc["variances"])
+    rel = (sv[:-1] - sv[1:]) / sv[1:]
+    gap = np.minimum(np.r_[np.inf, rel], np.r_[rel, np.inf])
+    for a, b in ((gpu.rotation, orc["rotation"]), (gpu.scores, orc["scores"])):
+        assert principal_sines(a, b).max() < 1e-8
+        sines = column_sines(a, b)
+        print("per-column sines: max %.2e; max sine x gap %.2e" % (sines.max(), (sines * gap).max()))
+        assert np.all(sines[gap >= 1e-4] < 1e-8)
+        assert np.all(sines * gap <= 1e-12)
     np.testing.assert_allclose(gpu.center, orc["center"], rtol=1e-12, atol=1e-15)
     np.testing.assert_allclose(gpu.scale, orc["scale"], rtol=1e-12)
 

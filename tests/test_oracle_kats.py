@@ -69,6 +69,48 @@ def test_svd_rank_deficient_completion(oracle_mod):
     np.testing.assert_allclose(U @ np.diag(S) @ V.T, A, atol=1e-12 * S[0])
 
 
+def _restart_shaped(n, k, seed):
+    # The shape of B after a restart (compute.hpp:282-293 then the Lanczos run):
+    # diagonal singular values, a residual column k, an upper-bidiagonal tail.
+    rng = np.random.default_rng(seed)
+    B = np.zeros((n, n))
+    B[np.arange(k), np.arange(k)] = np.sort(rng.uniform(1, 100, k))[::-1]
+    B[:k, k] = 1e-3 * rng.standard_normal(k)
+    for i in range(k, n):
+        B[i, i] = abs(rng.standard_normal())
+        if i + 1 < n:
+            B[i, i + 1] = abs(rng.standard_normal())
+    return B
+
+
+@pytest.mark.parametrize("case", ["1", "2", "7", "57", "64", "restart", "rank2", "zero", "ties"])
+def test_svd_square_two_sided(oracle_mod, case):
+    # The restart SVD (two-sided Jacobi as Eigen::JacobiSVD, compute.hpp:225).
+    if case == "restart":
+        A = _restart_shaped(57, 50, 3)
+    elif case == "rank2":
+        A = normal_matrix(30, 2, seed=4) @ normal_matrix(2, 30, seed=5)
+    elif case == "zero":
+        A = np.zeros((5, 5))
+    elif case == "ties":
+        A = np.diag([3.0, 1.0, 3.0, 2.0, 1.0])
+    else:
+        n = int(case)
+        A = normal_matrix(n, n, seed=n)
+    U, S, V = oracle_mod.svd_square(A)
+    n = A.shape[0]
+    ref = np.linalg.svd(A, compute_uv=False)
+    top = max(ref[0], 1.0)
+    np.testing.assert_allclose(S, ref, rtol=1e-13, atol=1e-13 * top)
+    assert np.all(np.diff(S) <= 0)
+    np.testing.assert_allclose(U @ np.diag(S) @ V.T, A, atol=1e-13 * top * max(n, 1))
+    np.testing.assert_allclose(U.T @ U, np.eye(n), atol=1e-13)
+    np.testing.assert_allclose(V.T @ V, np.eye(n), atol=1e-13)
+    # canonical signs: the largest-magnitude entry of each V column is positive
+    for j in range(n):
+        assert V[np.argmax(np.abs(V[:, j])), j] > 0
+
+
 def _lanczos_setup(nr, nc, work):
     rng = np.random.default_rng(42)
     A = rng.standard_normal((nr, nc))
