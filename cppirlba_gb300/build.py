@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "_lib")
 BUILD = os.path.join(HERE, "_lib", "obj")
 
 CUDA_SOURCES = ["engine.cu", "spmv.cu", "vec.cu", "svd.cu", "batch.cu", "batch_host.cu", "adjoint.cu",
-                "adjoint_host.cu", "ingest.cu", "staging.cu"]
+                "adjoint_host.cu", "ingest.cu", "staging.cu", "rotate_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O3", "-Xcompiler", "-pthread", "-Xcompiler", "-Wall",

@@ -72,6 +72,16 @@ void launch_epilogue(T* y, int64_t nrows, const Epilogue<T>& e, const int32_t* a
 cudaError_t spmv_configure(size_t max_smem);
 int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group, int shape = 0);
 cudaError_t rotate_configure(size_t max_smem);
+// The FP32 restart rotation on the tensor cores (rotate_tc.cu): w, k <= 64.
+cudaError_t rotate_tc_configure(size_t max_smem);
+bool rotate_tc32_available();
+size_t rotate_tc32_smem_bytes();
+void launch_rotate_tc32(const float* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                        float* out, int64_t ldo, const float* fcol, const double* fnorm, const int32_t* abort,
+                        int32_t* error_flag, int sms, cudaStream_t stream);
+// 1 if a tensor-core rotation since the last call gave up on a bounded wait
+// (its output is invalid), 0 if none did, -1 if the flag could not be read.
+int rotate_tc_take_error();
 int cgs_update_grid(int64_t L);
 int cgs_dot_grid(int64_t L);
 

@@ -1,0 +1,377 @@
+// The restart rotation of the FP32 form, out[:, :k] = Q[:, :w] R[:w, :k]
+// (compute.hpp:268-280: V <- V BV, W <- W BU), on the tcgen05 tensor cores.
+//
+// The product keeps FP32 accuracy through error-free BF16 splitting, the
+// scheme of Ozaki, Ogita, Oishi and Rump ("Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication",
+// Numerical Algorithms 59, 2012): every row r of Q is scaled by a power of two
+// 2^-e_r with 2^e_r above its largest magnitude and cut into three slices of
+// at most eight significant bits, x 2^-e_r = a0 2^-8 + a1 2^-16 + a2 2^-24 + r
+// with integers |a_s| <= 256 and |r| <= 2^-25 (each slice the nearest integer
+// of the scaled remainder); every column c of R likewise, with 2^-f_c and
+// slices b_t. The slices are exact in BF16 and their products exact in the
+// MMA's FP32 accumulators: |a_s b_t| <= 2^16, a sum over K = 64 stays below
+// 2^22 and the pairs (s, t) with s + t = d (at most three) sum below 2^24. The
+// six pairs with s + t <= 2 are kept (the rest fall below 2^-24 relative), in
+// three TMEM accumulators acc_d, and
+//   out[r, c] = 2^(e_r + f_c - 16) (acc_0 + 2^-8 (acc_1 + 2^-8 acc_2)).
+//
+// One persistent CTA per SM walks 128-row tiles: eight producer warps (two
+// groups of four, alternate tiles, one thread per row) load their rows of Q,
+// find the row exponent and write the three slices to a shared-memory buffer in
+// the no-swizzle K-major core-matrix layout; one thread issues the 24 MMAs of a
+// tile (M = 128, N = 64, K = 16, kind::f16 with BF16 operands and FP32
+// accumulation) and commits them to an mbarrier; four epilogue warps read the
+// three accumulators of their 32 rows from TMEM (tcgen05.ld), combine them and
+// store the output rows. Two slice buffers and two TMEM accumulator sets let
+// the loads and slicing of one tile overlap the MMAs and the epilogue of the
+// previous one. Every wait is bounded: on expiry the CTA records an error,
+// stops issuing work and frees its TMEM.
+//
+// Shared-memory layout of a 128 x 64 (or 64 x 64) BF16 operand: core matrices
+// of 8 rows x 16 bytes (eight K-consecutive elements), core (i, kc) at byte
+// (8 i + kc) 128; so the leading byte offset (between K-adjacent cores) is 128
+// and the stride byte offset (between row-adjacent cores) is 1024, and K-step
+// kk of 16 starts 256 kk bytes in.
+
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace irlba_gb300 {
+
+// Set by a rotation whose bounded waits expired (its output is then invalid);
+// read and cleared by rotate_tc_take_error().
+__device__ int32_t g_rotate_tc_error = 0;
+
+namespace {
+
+constexpr int kTcRows = 128;                                   // tile rows = MMA M
+constexpr int kTcK = 64;                                       // padded w (4 K-steps)
+constexpr int kTcN = 64;                                       // padded k = MMA N
+constexpr int kTcSlices = 3;
+constexpr uint32_t kTcSliceA = kTcRows * kTcK * 2;             // 16 KB
+constexpr uint32_t kTcSliceB = kTcN * kTcK * 2;                // 8 KB
+constexpr uint32_t kTcAccCols = 256;                           // one accumulator set (3 x 64 used)
+constexpr int kTcEpiWarps = 4, kTcProdWarps = 8;
+constexpr int kTcThreads = 32 * (kTcEpiWarps + kTcProdWarps + 1);
+constexpr long long kTcSpin = 1ll << 24;                       // bounded waits (polls)
+
+struct TcSmem {
+    alignas(1024) unsigned char A[2][kTcSlices][kTcSliceA];
+    alignas(1024) unsigned char B[kTcSlices][kTcSliceB];
+    float rowscale[2][kTcRows];
+    float colscale[kTcN];
+    alignas(8) unsigned long long full[2];
+    alignas(8) unsigned long long tfull[2];
+    alignas(8) unsigned long long tempty[2];
+    uint32_t tmem;
+    int err;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = static_cast<uint64_t>((addr & 0x3ffffu) >> 4);
+    d |= static_cast<uint64_t>(128u >> 4) << 16;     // leading byte offset: K-adjacent cores
+    d |= static_cast<uint64_t>(1024u >> 4) << 32;    // stride byte offset: row-adjacent cores
+    d |= static_cast<uint64_t>(1) << 46;             // descriptor version
+    return d;                                        // base offset 0, no swizzle
+}
+
+// Instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N, M.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(kTcN >> 3) << 17) |
+                              (static_cast<uint32_t>(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ int core_offset(int r, int k) {
+    return ((r >> 3) * 8 + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_addr(b)) : "memory");
+}
+// Waits for the phase with the given parity; false after kTcSpin polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity) {
+    uint32_t done = 0;
+    for (long long it = 0; it < kTcSpin; ++it) {
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(smem_addr(b)), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Nearest integer of y for |y| < 2^22 (adding and removing 1.5 * 2^23).
+__device__ __forceinline__ float round_int(float y) {
+    return __fsub_rn(__fadd_rn(y, 12582912.0f), 12582912.0f);
+}
+
+// The three slices of x (already scaled into (-1, 1)) as BF16 bit patterns.
+__device__ __forceinline__ void split3(float x, uint32_t& s0, uint32_t& s1, uint32_t& s2) {
+    const float y0 = __fmul_rn(x, 256.0f);
+    const float a0 = round_int(y0);
+    const float y1 = __fmul_rn(__fsub_rn(y0, a0), 256.0f);
+    const float a1 = round_int(y1);
+    const float y2 = __fmul_rn(__fsub_rn(y1, a1), 256.0f);
+    const float a2 = round_int(y2);
+    s0 = __float_as_uint(a0) >> 16;
+    s1 = __float_as_uint(a1) >> 16;
+    s2 = __float_as_uint(a2) >> 16;
+}
+
+// 2^e as an FP32 value, -126 <= e <= 127.
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
+// e with 2^e > m >= 0 (e = 0 for m = 0; rows or columns below 2^-100 are
+// treated as 2^-100 in size), and 2^-e.
+__device__ __forceinline__ int exponent_above(float m, float* inv) {
+    int e = 0;
+    if (m > 0.0f) frexpf(m, &e);   // m = f 2^e, f in [0.5, 1): 2^e > m
+    e = e < -100 ? -100 : e;
+    *inv = pow2f(-e);
+    return e;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    rotate_tc32_kernel(const float* Q, int64_t L, int64_t ldq, int32_t w, const double* __restrict__ R, int32_t ldr,
+                       int32_t k, float* out, int64_t ldo, const float* __restrict__ fcol, const double* fnorm,
+                       const int32_t* abort, int32_t* error_flag) {
+    extern __shared__ __align__(1024) unsigned char tc_raw[];
+    // 1024-byte alignment of the operand buffers inside the dynamic window.
+    TcSmem& S = *reinterpret_cast<TcSmem*>(tc_raw + ((1024 - (smem_addr(tc_raw) & 1023)) & 1023));
+    if (abort && *abort) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t ntiles = (L + kTcRows - 1) / kTcRows;
+
+    // Setup: R's slices and column scales, barriers, TMEM (512 columns).
+    if (tid < kTcN) {
+        const int c = tid;
+        float m = 0.0f;
+        for (int j = 0; j < w && c < k; ++j) m = fmaxf(m, fabsf(static_cast<float>(R[j + static_cast<int64_t>(c) * ldr])));
+        float inv;
+        const int f = exponent_above(m, &inv);
+        S.colscale[c] = pow2f(f - 8);
+        for (int j0 = 0; j0 < kTcK; j0 += 8) {
+            uint32_t p[kTcSlices][4];
+            for (int u = 0; u < 8; u += 2) {
+                uint32_t lo[kTcSlices], hi[kTcSlices];
+                const int ja = j0 + u, jb = j0 + u + 1;
+                const float xa = (ja < w && c < k) ? static_cast<float>(R[ja + static_cast<int64_t>(c) * ldr]) * inv : 0.0f;
+                const float xb = (jb < w && c < k) ? static_cast<float>(R[jb + static_cast<int64_t>(c) * ldr]) * inv : 0.0f;
+                split3(xa, lo[0], lo[1], lo[2]);
+                split3(xb, hi[0], hi[1], hi[2]);
+                for (int s = 0; s < kTcSlices; ++s) p[s][u / 2] = lo[s] | (hi[s] << 16);
+            }
+            for (int s = 0; s < kTcSlices; ++s)
+                *reinterpret_cast<uint4*>(S.B[s] + core_offset(c, j0)) = make_uint4(p[s][0], p[s][1], p[s][2], p[s][3]);
+        }
+    }
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&S.full[b], 32 * kTcProdWarps / 2);
+            mbar_init(&S.tfull[b], 1);
+            mbar_init(&S.tempty[b], 32 * kTcEpiWarps);
+        }
+        S.err = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem)),
+                     "r"(2 * kTcAccCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = S.tmem;
+
+    if (warp < kTcEpiWarps) {
+        // Epilogue: rows 32 warp + lane of each tile (TMEM lanes of this warp).
+        const float finv = fcol ? static_cast<float>(1.0 / *fnorm) : 0.0f;
+        int64_t i = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+            const int b = static_cast<int>(i & 1);
+            // full[b] too (already complete): orders the producers' row scales before the reads.
+            if (!mbar_wait(&S.tfull[b], static_cast<uint32_t>((i >> 1) & 1)) ||
+                !mbar_wait(&S.full[b], static_cast<uint32_t>((i >> 1) & 1))) {
+                atomicExch(&S.err, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int row = warp * 32 + lane;
+            const int64_t r = tile * kTcRows + row;
+            const float rs = S.rowscale[b][row];
+            const uint32_t base = tmem + static_cast<uint32_t>(b) * kTcAccCols + (static_cast<uint32_t>(warp * 32) << 16);
+            for (int c0 = 0; c0 < kTcN; c0 += 16) {
+                uint32_t v[3][16];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                        "[%16];"
+                        : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
+                          "=r"(v[d][6]), "=r"(v[d][7]), "=r"(v[d][8]), "=r"(v[d][9]), "=r"(v[d][10]), "=r"(v[d][11]),
+                          "=r"(v[d][12]), "=r"(v[d][13]), "=r"(v[d][14]), "=r"(v[d][15])
+                        : "r"(base + static_cast<uint32_t>(d * kTcN + c0)));
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (r < L) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int c = c0 + j;
+                        if (c < k) {
+                            const float a0 = __uint_as_float(v[0][j]), a1 = __uint_as_float(v[1][j]),
+                                        a2 = __uint_as_float(v[2][j]);
+                            const float s = fmaf(fmaf(a2, 0.00390625f, a1), 0.00390625f, a0);
+                            out[r + static_cast<int64_t>(c) * ldo] = (s * rs) * S.colscale[c];
+                        }
+                    }
+                }
+            }
+            if (fcol && r < L) out[r + static_cast<int64_t>(k) * ldo] = fcol[r] * finv;
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(&S.tempty[b]);
+        }
+    } else if (warp < kTcEpiWarps + kTcProdWarps) {
+        // Producers: group g takes the CTA's tiles i = g, g + 2, ... into buffer g.
+        const int pw = warp - kTcEpiWarps;
+        const int g = pw / (kTcProdWarps / 2);
+        const int row = (pw % (kTcProdWarps / 2)) * 32 + lane;
+        int64_t i = g;
+        for (int64_t tile = blockIdx.x + g * static_cast<int64_t>(gridDim.x); tile < ntiles;
+             tile += 2 * static_cast<int64_t>(gridDim.x), i += 2) {
+            if (i >= 2 && !mbar_wait(&S.tempty[g], static_cast<uint32_t>(((i >> 1) - 1) & 1))) {
+                atomicExch(&S.err, 1);
+                break;
+            }
+            if (S.err) break;
+            const int64_t r = tile * kTcRows + row;
+            float x[kTcK];
+            float m = 0.0f;
+#pragma unroll
+            for (int j = 0; j < kTcK; ++j) {
+                x[j] = (j < w && r < L) ? Q[r + static_cast<int64_t>(j) * ldq] : 0.0f;
+                m = fmaxf(m, fabsf(x[j]));
+            }
+            float inv;
+            const int e = exponent_above(m, &inv);
+            S.rowscale[g][row] = pow2f(e - 8);
+#pragma unroll
+            for (int j0 = 0; j0 < kTcK; j0 += 8) {
+                uint32_t p[kTcSlices][4];
+#pragma unroll
+                for (int u = 0; u < 8; u += 2) {
+                    uint32_t lo[kTcSlices], hi[kTcSlices];
+                    split3(x[j0 + u] * inv, lo[0], lo[1], lo[2]);
+                    split3(x[j0 + u + 1] * inv, hi[0], hi[1], hi[2]);
+#pragma unroll
+                    for (int s = 0; s < kTcSlices; ++s) p[s][u / 2] = lo[s] | (hi[s] << 16);
+                }
+#pragma unroll
+                for (int s = 0; s < kTcSlices; ++s)
+                    *reinterpret_cast<uint4*>(S.A[g][s] + core_offset(row, j0)) =
+                        make_uint4(p[s][0], p[s][1], p[s][2], p[s][3]);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&S.full[g]);
+        }
+    } else if (lane == 0) {
+        // MMA issue: accumulator d of set b collects the pairs s + t = d.
+        int64_t i = 0;
+        int64_t issued = -1;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+            const int b = static_cast<int>(i & 1);
+            if (!mbar_wait(&S.full[b], static_cast<uint32_t>((i >> 1) & 1))) {
+                atomicExch(&S.err, 1);
+                break;
+            }
+            if (i >= 2 && !mbar_wait(&S.tempty[b], static_cast<uint32_t>(((i >> 1) - 1) & 1))) {
+                atomicExch(&S.err, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int d = 0; d < 3; ++d) {
+                const uint32_t dcol = tmem + static_cast<uint32_t>(b) * kTcAccCols + static_cast<uint32_t>(d * kTcN);
+                int first = 1;
+                for (int s = 0; s <= d; ++s) {
+                    const int t = d - s;
+                    for (int kk = 0; kk < kTcK / 16; ++kk) {
+                        const uint64_t ad = smem_desc(smem_addr(S.A[b][s]) + kk * 256);
+                        const uint64_t bd = smem_desc(smem_addr(S.B[t]) + kk * 256);
+                        const uint32_t acc = first ? 0u : 1u;
+                        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
+                                     "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc));
+                        first = 0;
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&S.tfull[b]))
+                         : "memory");
+            issued = i;
+        }
+        // The last committed MMAs are complete before the TMEM is freed (the
+        // epilogue may have stopped early on an error).
+        if (issued >= 0 && !mbar_wait(&S.tfull[issued & 1], static_cast<uint32_t>((issued >> 1) & 1)))
+            atomicExch(&S.err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTcAccCols));
+    }
+    if (tid == 0 && S.err) atomicExch(error_flag ? error_flag : &g_rotate_tc_error, 1);
+}
+
+}  // namespace
+
+size_t rotate_tc32_smem_bytes() { return sizeof(TcSmem) + 1024; }
+
+static bool g_rotate_tc_ok = false;
+static int g_rotate_tc_sms = 0;
+
+cudaError_t rotate_tc_configure(size_t max_smem) {
+    g_rotate_tc_ok = false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+        cudaDeviceGetAttribute(&g_rotate_tc_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (max_smem < rotate_tc32_smem_bytes()) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(rotate_tc32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(rotate_tc32_smem_bytes()));
+    g_rotate_tc_ok = e == cudaSuccess;
+    return e;
+}
+
+bool rotate_tc32_available() { return g_rotate_tc_ok; }
+
+int rotate_tc_take_error() {
+    int32_t v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_rotate_tc_error, sizeof(v)) != cudaSuccess) return -1;
+    if (v) {
+        const int32_t zero = 0;
+        cudaMemcpyToSymbol(g_rotate_tc_error, &zero, sizeof(zero));
+    }
+    return v;
+}
+
+void launch_rotate_tc32(const float* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                        float* out, int64_t ldo, const float* fcol, const double* fnorm, const int32_t* abort,
+                        int32_t* error_flag, int sms, cudaStream_t stream) {
+    if (L <= 0) return;
+    if (sms <= 0) sms = g_rotate_tc_sms > 0 ? g_rotate_tc_sms : 1;
+    const int64_t tiles = (L + kTcRows - 1) / kTcRows;
+    const int grid = static_cast<int>(tiles < sms ? tiles : sms);
+    rotate_tc32_kernel<<<grid, kTcThreads, rotate_tc32_smem_bytes(), stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol,
+                                                                               fnorm, abort, error_flag);
+    count_launch();
+}
+
+}  // namespace irlba_gb300
