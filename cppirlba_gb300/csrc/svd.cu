@@ -326,7 +326,8 @@ constexpr int kRefMaxSteps = 8;
 constexpr int kRefMaxSweeps32 = 30;
 constexpr float kRefTol32 = 1e-6f;
 constexpr float kRefStop32 = 1e-4f;     // a sweep whose rotations all had |cos| below this is the last
-constexpr float kRefBigAngle = 1e-4f;   // |theta| above this: an exact rotation
+constexpr float kRefBigAngle = 1e-4f;   // |theta| above this: an exact rotation (first two steps)
+constexpr float kRefBigAngleLate = 1e-6f;   // the same from the third step on
 constexpr int kRefMaxBig = 256;         // exact rotations per step (the rest wait a step)
 constexpr int kRefOwn = (kRefMaxN + kRefCTAs - 1) / kRefCTAs;   // columns owned per CTA
 
@@ -351,8 +352,8 @@ struct RefSmem {
     float lamf[kRefMaxN];            // C_jj / max C
     float rsqf[kRefMaxN];            // (C_jj / max C)^(-1/2), 0 for null columns
     double inv_lmax;
-    float maxima[2 * kRefCTAs];      // per CTA: max relative off-diagonal of C, max |E|
-    float redf[64];
+    float maxima[3 * kRefCTAs];      // per CTA: max relative off-diagonal of C, max |E|, max |theta|
+    float redf[96];
     double big_c[kRefMaxBig], big_s[kRefMaxBig];
     unsigned char big_p[kRefMaxBig], big_q[kRefMaxBig];
     int big_cnt[kRefMaxN];           // large angles in column q, then their offsets
@@ -465,25 +466,30 @@ __device__ int jacobi32_sweeps(float4* G, float4* V, const unsigned short* ptab,
     return sweep + 1;
 }
 
-// Maxima of two non-negative values over the CTA, valid in every thread. red:
-// 64 floats not otherwise in use until the CTA's next barrier after this call.
-__device__ void ref_block_max2f(float& x, float& y, float* red) {
+// Maxima of three non-negative values over the CTA, valid in every thread.
+// red: 96 floats not otherwise in use until the CTA's next barrier after this
+// call.
+__device__ void ref_block_max3f(float& x, float& y, float& z, float* red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, o));
         y = fmaxf(y, __shfl_xor_sync(0xffffffffu, y, o));
+        z = fmaxf(z, __shfl_xor_sync(0xffffffffu, z, o));
     }
     if (lane == 0) {
         red[warp] = x;
         red[32 + warp] = y;
+        red[64 + warp] = z;
     }
     __syncthreads();
     x = 0.f;
     y = 0.f;
+    z = 0.f;
     for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
         x = fmaxf(x, red[w]);
         y = fmaxf(y, red[32 + w]);
+        z = fmaxf(z, red[64 + w]);
     }
 }
 
@@ -717,7 +723,7 @@ __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
         // (b) Gram entries of the own columns: C_pq, N_pq in FP64, four lanes
         // per entry (rows i = l, l + 4, ...), so the FP64 work spreads over all
         // warps; E_pq and theta_pq to every CTA (each lane of the four writes two).
-        float offmax = 0.f, emax = 0.f;
+        float offmax = 0.f, emax = 0.f, thmax = 0.f;
         const int q4 = tid & 3;
         const double il = S.inv_lmax;
         for (int it0 = 0; it0 < nitems; it0 += static_cast<int>(blockDim.x >> 2)) {
@@ -765,6 +771,7 @@ __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
                         den = 1.f;
                     }
                     if (num != 0.f) th = den == 0.f ? copysignf(0.78539816f, num) : 0.5f * atanf(2.f * num / den);
+                    thmax = fmaxf(thmax, fabsf(th));
                 }
             }
             th = __shfl_sync(0xffffffffu, th, lane & ~3);
@@ -776,17 +783,19 @@ __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
                 }
             }
         }
-        ref_block_max2f(offmax, emax, S.redf);
+        ref_block_max3f(offmax, emax, thmax, S.redf);
         if (tid < kRefCTAs) {
             float* mr = cl.map_shared_rank(S.maxima, tid);
-            mr[2 * rank] = offmax;
-            mr[2 * rank + 1] = emax;
+            mr[3 * rank] = offmax;
+            mr[3 * rank + 1] = emax;
+            mr[3 * rank + 2] = thmax;
         }
         cl.sync();
-        float goff = 0.f, gem = 0.f;
+        float goff = 0.f, gem = 0.f, gth = 0.f;
         for (int r = 0; r < kRefCTAs; ++r) {
-            goff = fmaxf(goff, S.maxima[2 * r]);
-            gem = fmaxf(gem, S.maxima[2 * r + 1]);
+            goff = fmaxf(goff, S.maxima[3 * r]);
+            gem = fmaxf(gem, S.maxima[3 * r + 1]);
+            gth = fmaxf(gth, S.maxima[3 * r + 2]);
         }
         // Converged at 8 eps; or, once below the one-sided Jacobi's skip
         // threshold n eps, as soon as a step no longer shrinks the coupling by
@@ -800,64 +809,71 @@ __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
         prev_off = goff;
         if (steps == kRefMaxSteps) break;
 
-        // (c) The large angles in a fixed order (column q, then row p): counts
-        // per column, their offsets, then the entries (one warp per column).
-        for (int q = warp; q < n; q += nw) {
-            int cnt = 0;
-            for (int p0 = 0; p0 < q; p0 += 32) {
-                const int p = p0 + lane;
-                cnt += __popc(__ballot_sync(0xffffffffu, p < q && fabsf(EK[q * kRefLd + p].y) > kRefBigAngle));
+        // (c) The large angles (above 1e-4 in the first two steps, where the
+        // FP32 stage leaves them, 1e-6 later, where exact rotations settle the
+        // last clusters of close singular values) in a fixed order (column q,
+        // then row p): counts per column, their offsets, then the entries (one
+        // warp per column). Skipped when no angle is that large.
+        const float big = steps < 2 ? kRefBigAngle : kRefBigAngleLate;
+        int nbig = 0;
+        if (gth > big) {
+            for (int q = warp; q < n; q += nw) {
+                int cnt = 0;
+                for (int p0 = 0; p0 < q; p0 += 32) {
+                    const int p = p0 + lane;
+                    cnt += __popc(__ballot_sync(0xffffffffu, p < q && fabsf(EK[q * kRefLd + p].y) > big));
+                }
+                if (lane == 0) S.big_cnt[q] = cnt;
             }
-            if (lane == 0) S.big_cnt[q] = cnt;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            const int c0 = lane < n ? S.big_cnt[lane] : 0;
-            const int c1 = lane + 32 < n ? S.big_cnt[lane + 32] : 0;
-            int s0 = c0, s1 = c1;
+            __syncthreads();
+            if (warp == 0) {
+                const int c0 = lane < n ? S.big_cnt[lane] : 0;
+                const int c1 = lane + 32 < n ? S.big_cnt[lane + 32] : 0;
+                int s0 = c0, s1 = c1;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t0 = __shfl_up_sync(0xffffffffu, s0, o), t1 = __shfl_up_sync(0xffffffffu, s1, o);
-                if (lane >= o) {
-                    s0 += t0;
-                    s1 += t1;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t0 = __shfl_up_sync(0xffffffffu, s0, o), t1 = __shfl_up_sync(0xffffffffu, s1, o);
+                    if (lane >= o) {
+                        s0 += t0;
+                        s1 += t1;
+                    }
+                }
+                const int tot0 = __shfl_sync(0xffffffffu, s0, 31), tot1 = __shfl_sync(0xffffffffu, s1, 31);
+                __syncwarp();
+                if (lane < n) S.big_cnt[lane] = s0 - c0;
+                if (lane + 32 < n) S.big_cnt[lane + 32] = tot0 + s1 - c1;
+                if (lane == 0) S.nbig = tot0 + tot1 < kRefMaxBig ? tot0 + tot1 : kRefMaxBig;
+            }
+            __syncthreads();
+            for (int q = warp; q < n; q += nw) {
+                int base = S.big_cnt[q];
+                for (int p0 = 0; p0 < q; p0 += 32) {
+                    const int p = p0 + lane;
+                    const bool isbig = p < q && fabsf(EK[q * kRefLd + p].y) > big;
+                    const unsigned m = __ballot_sync(0xffffffffu, isbig);
+                    const int slot = base + __popc(m & ((1u << lane) - 1u));
+                    if (isbig && slot < kRefMaxBig) {
+                        S.big_p[slot] = static_cast<unsigned char>(p);
+                        S.big_q[slot] = static_cast<unsigned char>(q);
+                    }
+                    base += __popc(m);
                 }
             }
-            const int tot0 = __shfl_sync(0xffffffffu, s0, 31), tot1 = __shfl_sync(0xffffffffu, s1, 31);
-            __syncwarp();
-            if (lane < n) S.big_cnt[lane] = s0 - c0;
-            if (lane + 32 < n) S.big_cnt[lane + 32] = tot0 + s1 - c1;
-            if (lane == 0) S.nbig = tot0 + tot1 < kRefMaxBig ? tot0 + tot1 : kRefMaxBig;
-        }
-        __syncthreads();
-        for (int q = warp; q < n; q += nw) {
-            int base = S.big_cnt[q];
-            for (int p0 = 0; p0 < q; p0 += 32) {
-                const int p = p0 + lane;
-                const bool big = p < q && fabsf(EK[q * kRefLd + p].y) > kRefBigAngle;
-                const unsigned m = __ballot_sync(0xffffffffu, big);
-                const int slot = base + __popc(m & ((1u << lane) - 1u));
-                if (big && slot < kRefMaxBig) {
-                    S.big_p[slot] = static_cast<unsigned char>(p);
-                    S.big_q[slot] = static_cast<unsigned char>(q);
-                }
-                base += __popc(m);
+            __syncthreads();
+            nbig = S.nbig;
+            // Cosines and sines of the large angles: FP32 sincos, then scaled to
+            // c^2 + s^2 = 1 in FP64 ((1 + d)^(-1/2) to second order in d ~ 1e-7).
+            for (int b = tid; b < nbig; b += blockDim.x) {
+                float s32, c32;
+                sincosf(EK[S.big_q[b] * kRefLd + S.big_p[b]].y, &s32, &c32);
+                const double c = c32, s = s32;
+                const double d = fma(c, c, fma(s, s, -1.0));
+                const double f = fma(0.375 * d, d, fma(-0.5, d, 1.0));
+                S.big_c[b] = c * f;
+                S.big_s[b] = s * f;
             }
+            __syncthreads();
         }
-        __syncthreads();
-        const int nbig = S.nbig;
-        // Cosines and sines of the large angles: FP32 sincos, then scaled to
-        // c^2 + s^2 = 1 in FP64 ((1 + d)^(-1/2) to second order in d ~ 1e-7).
-        for (int b = tid; b < nbig; b += blockDim.x) {
-            float s32, c32;
-            sincosf(EK[S.big_q[b] * kRefLd + S.big_p[b]].y, &s32, &c32);
-            const double c = c32, s = s32;
-            const double d = fma(c, c, fma(s, s, -1.0));
-            const double f = fma(0.375 * d, d, fma(-0.5, d, 1.0));
-            S.big_c[b] = c * f;
-            S.big_s[b] = s * f;
-        }
-        __syncthreads();
         // The full E (symmetric) and K (skew, large angles removed) in FP32:
         // each thread completes one pair (p < q) or a diagonal entry.
         for (int e = tid; e < n * (n + 1) / 2; e += blockDim.x) {
@@ -867,7 +883,7 @@ __global__ void __cluster_dims__(kRefCTAs, 1, 1) __launch_bounds__(kRefThreads)
             while ((q + 1) * (q + 2) / 2 <= e) ++q;
             const int p = e - q * (q + 1) / 2;
             float2 v = EK[q * kRefLd + p];
-            if (p == q || fabsf(v.y) > kRefBigAngle) v.y = 0.f;
+            if (p == q || fabsf(v.y) > big) v.y = 0.f;
             EK[q * kRefLd + p] = v;
             if (p != q) EK[p * kRefLd + q] = make_float2(v.x, -v.y);
         }
