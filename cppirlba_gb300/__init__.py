@@ -154,6 +154,8 @@ def load_library():
         "irlba_gb300_set_profiling": (None, [i32]),
         "irlba_gb300_set_device_ingest": (None, [i32]),
         "irlba_gb300_set_spmv_shape": (None, [i32]),
+        "irlba_gb300_set_rotation_engine": (None, [i32]),
+        "irlba_gb300_rotate_device": (i32, [i32, P, i64, i64, i32, P, i32, i32, P, i64, P, P, i32, P]),
         "irlba_gb300_set_staging": (None, [i64, i64]),
         "irlba_gb300_last_profile": (None, [pd, ctypes.POINTER(i64)]),
         "irlba_gb300_launch_count": (i64, []),
@@ -592,6 +594,12 @@ def set_spmv_shape(shape):
     afterwards: 0 = 256-thread CTAs, 1 = 256 threads six per SM, 2 (default) =
     512 threads three per SM."""
     load_library().irlba_gb300_set_spmv_shape(int(shape))
+
+
+def set_rotation_engine(engine):
+    """Engine of the restart rotations (w, k <= 64) of later compute calls:
+    1 = tensor cores (default), 0 = CUDA cores."""
+    load_library().irlba_gb300_set_rotation_engine(int(engine))
 
 
 def set_staging(min_bytes=16 << 20, slice_bytes=8 << 20):

@@ -220,6 +220,58 @@ __global__ void shift_kernel(int64_t L, int k, const double* __restrict__ shift,
         Q[e] = shift[e % k] * P[e] - W[e];
 }
 
+// CG scalars of the shifted complement solves, kept on the device so the
+// iterations run without a host round trip. st: [0] columns still active,
+// [1] a non-positive curvature was met, [2] iterations that had an active
+// column. One CTA of at least k threads.
+__global__ void cg_init_kernel(int k, const double* __restrict__ rr0, double* rr, double* bnorm, int32_t* active,
+                               int32_t* st) {
+    const int j = threadIdx.x;
+    int a = 0;
+    if (j < k) {
+        rr[j] = rr0[j];
+        bnorm[j] = sqrt(rr0[j]);
+        a = bnorm[j] > 0;
+        active[j] = a;
+    }
+    a = __syncthreads_or(a);
+    if (j == 0) {
+        st[0] = a;
+        st[1] = 0;
+        st[2] = 0;
+    }
+}
+
+// alpha_j = rr_j / (p_j . q_j) for the active columns, 0 otherwise.
+__global__ void cg_alpha_kernel(int k, const double* __restrict__ pq, const double* __restrict__ rr,
+                                const int32_t* __restrict__ active, double* alpha, int32_t* st) {
+    const int j = threadIdx.x;
+    if (j == 0 && st[0]) st[2] += 1;
+    if (j >= k) return;
+    double a = 0;
+    if (active[j]) {
+        if (pq[j] > 0) a = rr[j] / pq[j];
+        else st[1] = 1;
+    }
+    alpha[j] = a;
+}
+
+// Columns with ||r_j|| <= tol ||b_j|| stop; beta_j = rn_j / rr_j for the rest.
+__global__ void cg_beta_kernel(int k, const double* __restrict__ rn, double* rr, const double* __restrict__ bnorm,
+                               double tol, int32_t* active, double* beta, int32_t* st) {
+    const int j = threadIdx.x;
+    int a = 0;
+    if (j < k) {
+        a = active[j];
+        if (a && sqrt(rn[j]) <= tol * bnorm[j]) a = 0;
+        active[j] = a;
+        beta[j] = a ? rn[j] / rr[j] : 0.0;
+        rr[j] = rn[j];
+    }
+    a = __syncthreads_or(a);
+    if (j == 0) st[0] = a;
+}
+
 // Column-major (ld) -> row-major (L x k) copy, optional; NULL source gives zeros.
 __global__ void to_rows_kernel(int64_t L, int k, const double* __restrict__ src, int64_t ld, double* out) {
     for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < L * k;
@@ -396,6 +448,24 @@ void launch_scale_rows(int64_t L, int k, const double* X, const double* sv, int 
 void launch_cg_step(int64_t L, int k, const double* alpha, const double* P, const double* Q, double* X, double* R,
                     cudaStream_t s) {
     cg_step_kernel<<<grid_of(L * k, kT, 152 * 8), kT, 0, s>>>(L, k, alpha, P, Q, X, R);
+    count_launch();
+}
+
+void launch_cg_init(int k, const double* rr0, double* rr, double* bnorm, int32_t* active, int32_t* st,
+                    cudaStream_t s) {
+    cg_init_kernel<<<1, kAdjointMaxK, 0, s>>>(k, rr0, rr, bnorm, active, st);
+    count_launch();
+}
+
+void launch_cg_alpha(int k, const double* pq, const double* rr, const int32_t* active, double* alpha, int32_t* st,
+                     cudaStream_t s) {
+    cg_alpha_kernel<<<1, kAdjointMaxK, 0, s>>>(k, pq, rr, active, alpha, st);
+    count_launch();
+}
+
+void launch_cg_beta(int k, const double* rn, double* rr, const double* bnorm, double tol, int32_t* active,
+                    double* beta, int32_t* st, cudaStream_t s) {
+    cg_beta_kernel<<<1, kAdjointMaxK, 0, s>>>(k, rn, rr, bnorm, tol, active, beta, st);
     count_launch();
 }
 

@@ -108,73 +108,70 @@ void put(double* d, const std::vector<double>& h, cudaStream_t s) {
 
 // Solves (shift_j I - Op) x_j = b_j for every column j by conjugate gradients,
 // Op = P A'A'^T P (left) or P A'^T A' P (right), P the projector off the basis
-// Qb. Columns stop when ||r_j|| <= tol ||b_j||. Returns the iteration count.
+// Qb. Columns stop when ||r_j|| <= tol ||b_j||. The CG scalars live on the
+// device (launch_cg_alpha / launch_cg_beta), so iterations are issued in
+// groups of kCgCheck without a host round trip; the host reads the status
+// once per group. Iterations issued after every column has stopped change
+// nothing (alpha = 0 leaves X and R as they are). Returns the number of
+// iterations that had an active column.
+constexpr int kCgCheck = 8;
+
 int shifted_cg(BlockOp& op, bool left, const double* Qb, const double* B, const std::vector<double>& shift, double tol,
                int max_iter, double* X, cudaStream_t s) {
     const int k = op.k;
     const int64_t L = left ? op.m : op.n, O = left ? op.n : op.m;
     DevBuf R(sizeof(double) * L * k), P(sizeof(double) * L * k), Q(sizeof(double) * L * k),
         W(sizeof(double) * L * k), T(sizeof(double) * std::max<int64_t>(O * k, 1)), G(sizeof(double) * k * k),
-        part(sizeof(double) * static_cast<int64_t>(gram_parts(L)) * k * k), dv(sizeof(double) * k),
-        dshift(sizeof(double) * k);
+        part(sizeof(double) * static_cast<int64_t>(gram_parts(L)) * k * k), dshift(sizeof(double) * k),
+        scal(sizeof(double) * 6 * kAdjointMaxK), flags(sizeof(int32_t) * (kAdjointMaxK + 4));
+    double* dv = scal.as<double>();                  // coldot outputs
+    double* rr = dv + kAdjointMaxK;
+    double* bnorm = dv + 2 * kAdjointMaxK;
+    double* alpha = dv + 3 * kAdjointMaxK;
+    double* beta = dv + 4 * kAdjointMaxK;
+    int32_t* st = flags.as<int32_t>();
+    int32_t* active = st + 4;
     put(dshift.as<double>(), shift, s);
     CUDA_TRY(cudaMemsetAsync(X, 0, sizeof(double) * L * k, s));
     CUDA_TRY(cudaMemcpyAsync(R.ptr, B, sizeof(double) * L * k, cudaMemcpyDeviceToDevice, s));
     CUDA_TRY(cudaMemcpyAsync(P.ptr, B, sizeof(double) * L * k, cudaMemcpyDeviceToDevice, s));
-    launch_coldot(R.as<double>(), R.as<double>(), nullptr, L, k, part.as<double>(), dv.as<double>(), s);
-    std::vector<double> rr = fetch(dv.as<double>(), k, s);
-    std::vector<double> bnorm(k), alpha(k), beta(k);
-    std::vector<char> active(k);
-    bool any = false;
-    for (int j = 0; j < k; ++j) {
-        bnorm[j] = std::sqrt(rr[j]);
-        active[j] = bnorm[j] > 0;
-        any = any || active[j];
+    launch_coldot(R.as<double>(), R.as<double>(), nullptr, L, k, part.as<double>(), dv, s);
+    launch_cg_init(k, dv, rr, bnorm, active, st, s);
+    int32_t hst[3] = {0, 0, 0};
+    CUDA_TRY(d2h_async(hst, st, sizeof(hst), s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    int issued = 0;
+    while (hst[0] && issued < max_iter) {
+        const int group = std::min(kCgCheck, max_iter - issued);
+        for (int g = 0; g < group; ++g, ++issued) {
+            project_out(Qb, L, k, P.as<double>(), G.as<double>(), part.as<double>(), s);
+            if (left) {
+                op.adj(P.as<double>(), T.as<double>());
+                op.mul(T.as<double>(), W.as<double>());
+            } else {
+                op.mul(P.as<double>(), T.as<double>());
+                op.adj(T.as<double>(), W.as<double>());
+            }
+            project_out(Qb, L, k, W.as<double>(), G.as<double>(), part.as<double>(), s);
+            launch_shift(L, k, dshift.as<double>(), P.as<double>(), W.as<double>(), Q.as<double>(), s);
+            launch_coldot(P.as<double>(), Q.as<double>(), nullptr, L, k, part.as<double>(), dv, s);
+            launch_cg_alpha(k, dv, rr, active, alpha, st, s);
+            launch_cg_step(L, k, alpha, P.as<double>(), Q.as<double>(), X, R.as<double>(), s);
+            launch_coldot(R.as<double>(), R.as<double>(), nullptr, L, k, part.as<double>(), dv, s);
+            launch_cg_beta(k, dv, rr, bnorm, tol, active, beta, st, s);
+            launch_cg_dir(L, k, beta, R.as<double>(), P.as<double>(), s);
+        }
+        CUDA_TRY(d2h_async(hst, st, sizeof(hst), s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        if (hst[1])
+            throw Error(IRLBA_GB300_ERROR_NUMERICAL,
+                        "the SVD adjoint needs the k-th singular value to exceed the (k+1)-th "
+                        "(complement system not positive definite)");
     }
-    int it = 0;
-    while (any && it < max_iter) {
-        ++it;
-        project_out(Qb, L, k, P.as<double>(), G.as<double>(), part.as<double>(), s);
-        if (left) {
-            op.adj(P.as<double>(), T.as<double>());
-            op.mul(T.as<double>(), W.as<double>());
-        } else {
-            op.mul(P.as<double>(), T.as<double>());
-            op.adj(T.as<double>(), W.as<double>());
-        }
-        project_out(Qb, L, k, W.as<double>(), G.as<double>(), part.as<double>(), s);
-        launch_shift(L, k, dshift.as<double>(), P.as<double>(), W.as<double>(), Q.as<double>(), s);
-        launch_coldot(P.as<double>(), Q.as<double>(), nullptr, L, k, part.as<double>(), dv.as<double>(), s);
-        const std::vector<double> pq = fetch(dv.as<double>(), k, s);
-        for (int j = 0; j < k; ++j) {
-            alpha[j] = 0;
-            if (!active[j]) continue;
-            if (!(pq[j] > 0))
-                throw Error(IRLBA_GB300_ERROR_NUMERICAL,
-                            "the SVD adjoint needs the k-th singular value to exceed the (k+1)-th "
-                            "(complement system not positive definite)");
-            alpha[j] = rr[j] / pq[j];
-        }
-        put(dv.as<double>(), alpha, s);
-        launch_cg_step(L, k, dv.as<double>(), P.as<double>(), Q.as<double>(), X, R.as<double>(), s);
-        launch_coldot(R.as<double>(), R.as<double>(), nullptr, L, k, part.as<double>(), dv.as<double>(), s);
-        const std::vector<double> rn = fetch(dv.as<double>(), k, s);
-        any = false;
-        for (int j = 0; j < k; ++j) {
-            if (active[j] && std::sqrt(rn[j]) <= tol * bnorm[j]) active[j] = 0;
-            beta[j] = active[j] ? rn[j] / rr[j] : 0.0;
-            any = any || active[j];
-            rr[j] = rn[j];
-        }
-        if (!any) break;
-        put(dv.as<double>(), beta, s);
-        launch_cg_dir(L, k, dv.as<double>(), R.as<double>(), P.as<double>(), s);
-    }
-    if (any)
+    if (hst[0])
         throw Error(IRLBA_GB300_ERROR_NUMERICAL,
                     "the SVD adjoint's complement solve did not reach its tolerance within the iteration limit");
-    CUDA_TRY(cudaStreamSynchronize(s));
-    return it;
+    return hst[2];
 }
 
 }  // namespace

@@ -959,7 +959,7 @@ struct Engine {
         CUDA_TRY(cudaEventRecord(ev1, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         CUDA_TRY(cudaGetLastError());
-        if (std::is_same<T, float>::value && rotate_tc_take_error() != 0)
+        if (rotate_tc_take_error() != 0)
             throw Error(IRLBA_GB300_ERROR_CUDA, "a tensor-core basis rotation timed out on a wait");
         float dev_ms = 0;
         cudaEventElapsedTime(&dev_ms, ev0, ev1);
@@ -1651,6 +1651,41 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
 }
 
 void irlba_gb300_set_device_ingest(int32_t on) { g_device_ingest = on != 0; }
+void irlba_gb300_set_rotation_engine(int32_t engine) { set_rotate_engine(engine); }
+
+irlba_gb300_status irlba_gb300_rotate_device(int32_t fp64, const void* Q, int64_t L, int64_t ldq, int32_t w,
+                                             const double* R, int32_t ldr, int32_t k, void* out, int64_t ldo,
+                                             const void* fcol, const double* fnorm, int32_t engine, void* stream) {
+    return guarded([&]() {
+        if (L < 0 || w < 0 || k < 0) invalid("sizes must be non-negative");
+        if (!Q || !R || !out) invalid("NULL argument");
+        if (ldq < L || ldo < L || ldr < w) invalid("leading dimension is smaller than the extent");
+        if (fcol && !fnorm) invalid("fcol needs fnorm");
+        if (engine == 1 && (w < 1 || w > 64 || k > 64))
+            throw Error(IRLBA_GB300_ERROR_UNSUPPORTED, "tensor-core rotations take 1 <= w <= 64, k <= 64");
+        device_info();
+        if (engine == 1 && !(fp64 ? rotate_tc64_available() : rotate_tc32_available()))
+            throw Error(IRLBA_GB300_ERROR_UNSUPPORTED, "tensor-core rotation not available on this device");
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (fp64) {
+            const double* q = static_cast<const double*>(Q);
+            double* o = static_cast<double*>(out);
+            const double* f = static_cast<const double*>(fcol);
+            if (engine == 1) launch_rotate_tc64(q, L, ldq, w, R, ldr, k, o, ldo, f, fnorm, nullptr, nullptr, 0, s);
+            else launch_rotate_cores<double>(q, L, ldq, w, R, ldr, k, o, ldo, f, fnorm, nullptr, s);
+        } else {
+            const float* q = static_cast<const float*>(Q);
+            float* o = static_cast<float*>(out);
+            const float* f = static_cast<const float*>(fcol);
+            if (engine == 1) launch_rotate_tc32(q, L, ldq, w, R, ldr, k, o, ldo, f, fnorm, nullptr, nullptr, 0, s);
+            else launch_rotate_cores<float>(q, L, ldq, w, R, ldr, k, o, ldo, f, fnorm, nullptr, s);
+        }
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamSynchronize(s));
+        if (rotate_tc_take_error() != 0) throw Error(IRLBA_GB300_ERROR_CUDA, "a tensor-core rotation timed out on a wait");
+    });
+}
+
 void irlba_gb300_set_spmv_shape(int32_t shape) { g_spmv_shape = shape >= 0 && shape <= 2 ? shape : 2; }
 
 irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, const void* values,

@@ -72,13 +72,23 @@ void launch_epilogue(T* y, int64_t nrows, const Epilogue<T>& e, const int32_t* a
 cudaError_t spmv_configure(size_t max_smem);
 int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group, int shape = 0);
 cudaError_t rotate_configure(size_t max_smem);
-// The FP32 restart rotation on the tensor cores (rotate_tc.cu): w, k <= 64.
+// The restart rotations on the tensor cores (rotate_tc.cu): w, k <= 64, FP32
+// (three BF16 slices) and FP64 (seven) forms; out may be Q (rows are read
+// before they are written). error_flag NULL: a module-wide flag.
 cudaError_t rotate_tc_configure(size_t max_smem);
 bool rotate_tc32_available();
+bool rotate_tc64_available();
 size_t rotate_tc32_smem_bytes();
+size_t rotate_tc64_smem_bytes();
 void launch_rotate_tc32(const float* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
                         float* out, int64_t ldo, const float* fcol, const double* fnorm, const int32_t* abort,
                         int32_t* error_flag, int sms, cudaStream_t stream);
+void launch_rotate_tc64(const double* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                        double* out, int64_t ldo, const double* fcol, const double* fnorm, const int32_t* abort,
+                        int32_t* error_flag, int sms, cudaStream_t stream);
+// Engine of the restart rotations with w, k <= 64: 1 = tensor cores (default), 0 = CUDA cores.
+void set_rotate_engine(int engine);
+int rotate_engine();
 // 1 if a tensor-core rotation since the last call gave up on a bounded wait
 // (its output is invalid), 0 if none did, -1 if the flag could not be read.
 int rotate_tc_take_error();
@@ -121,6 +131,12 @@ void launch_beta(const T* x, int64_t L, const T* fscale, int32_t fdivide, const 
 template <typename T>
 void launch_rotate(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, T* out,
                    int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream);
+
+// Same, on the CUDA cores whatever the rotation engine setting.
+template <typename T>
+void launch_rotate_cores(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                         T* out, int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort,
+                         cudaStream_t stream);
 
 // Same, writing FP64 output (the final U and V).
 template <typename T>
@@ -291,6 +307,15 @@ void launch_scale_rows(int64_t L, int k, const double* X, const double* sv, int 
 void launch_cg_step(int64_t L, int k, const double* alpha, const double* P, const double* Q, double* X, double* R,
                     cudaStream_t s);
 void launch_cg_dir(int64_t L, int k, const double* beta, const double* R, double* P, cudaStream_t s);
+// Device-side CG scalars (k <= kAdjointMaxK): st[0] columns active, st[1]
+// non-positive curvature met, st[2] iterations with an active column.
+void launch_cg_init(int k, const double* rr0, double* rr, double* bnorm, int32_t* active, int32_t* st,
+                    cudaStream_t s);
+void launch_cg_alpha(int k, const double* pq, const double* rr, const int32_t* active, double* alpha, int32_t* st,
+                     cudaStream_t s);
+void launch_cg_beta(int k, const double* rn, double* rr, const double* bnorm, double tol, int32_t* active,
+                    double* beta, int32_t* st, cudaStream_t s);
+
 void launch_shift(int64_t L, int k, const double* shift, const double* P, const double* W, double* Q, cudaStream_t s);
 void launch_to_rows(int64_t L, int k, const double* src, int64_t ld, double* out, cudaStream_t s);
 // d[r] = coef * X[r, :] . (Y ? Y[r, :] : y)

@@ -28,6 +28,10 @@
 // previous one. Every wait is bounded: on expiry the CTA records an error,
 // stops issuing work and frees its TMEM.
 //
+// The FP64 form's rotation (rotate_tc64_kernel, below) uses the same scheme
+// with seven slices of eight bits taken from an exact fixed-point image of each
+// FP64 value and 28 slice pairs, accurate to the FP64 rounding level.
+//
 // Shared-memory layout of a 128 x 64 (or 64 x 64) BF16 operand: core matrices
 // of 8 rows x 16 bytes (eight K-consecutive elements), core (i, kc) at byte
 // (8 i + kc) 128; so the leading byte offset (between K-adjacent cores) is 128
@@ -55,13 +59,15 @@ constexpr uint32_t kTcSliceB = kTcN * kTcK * 2;                // 8 KB
 constexpr uint32_t kTcAccCols = 256;                           // one accumulator set (3 x 64 used)
 constexpr int kTcEpiWarps = 4, kTcProdWarps = 8;
 constexpr int kTcThreads = 32 * (kTcEpiWarps + kTcProdWarps + 1);
-constexpr long long kTcSpin = 1ll << 24;                       // bounded waits (polls)
+constexpr long long kTcWaitCycles = 4000000000ll;              // bounded waits: about 2 s of SM clock
 
 struct TcSmem {
     alignas(1024) unsigned char A[2][kTcSlices][kTcSliceA];
     alignas(1024) unsigned char B[kTcSlices][kTcSliceB];
     float rowscale[2][kTcRows];
     float colscale[kTcN];
+    float colinv[kTcN];
+    uint32_t colmax[kTcN];
     alignas(8) unsigned long long full[2];
     alignas(8) unsigned long long tfull[2];
     alignas(8) unsigned long long tempty[2];
@@ -95,15 +101,17 @@ __device__ __forceinline__ void mbar_init(unsigned long long* b, uint32_t count)
 __device__ __forceinline__ void mbar_arrive(unsigned long long* b) {
     asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_addr(b)) : "memory");
 }
-// Waits for the phase with the given parity; false after kTcSpin polls.
+// Waits for the phase with the given parity; false once kTcWaitCycles SM
+// cycles have passed without it.
 __device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity) {
     uint32_t done = 0;
-    for (long long it = 0; it < kTcSpin; ++it) {
+    const long long t0 = clock64();
+    while (true) {
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
                      : "=r"(done) : "r"(smem_addr(b)), "r"(parity) : "memory");
         if (done) return true;
+        if (clock64() - t0 > kTcWaitCycles) return false;
     }
-    return false;
 }
 
 // Nearest integer of y for |y| < 2^22 (adding and removing 1.5 * 2^23).
@@ -148,28 +156,30 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t ntiles = (L + kTcRows - 1) / kTcRows;
 
-    // Setup: R's slices and column scales, barriers, TMEM (512 columns).
+    // Setup: R's column scales (a shared maximum) and slices, spread over the
+    // whole CTA with consecutive threads on consecutive rows of a column.
+    if (tid < kTcN) S.colmax[tid] = 0u;
+    __syncthreads();
+    for (int e = tid; e < kTcN * kTcK; e += blockDim.x) {
+        const int c = e / kTcK, j = e % kTcK;
+        if (c < k && j < w)
+            atomicMax(&S.colmax[c], __float_as_uint(fabsf(static_cast<float>(R[j + static_cast<int64_t>(c) * ldr]))));
+    }
+    __syncthreads();
     if (tid < kTcN) {
-        const int c = tid;
-        float m = 0.0f;
-        for (int j = 0; j < w && c < k; ++j) m = fmaxf(m, fabsf(static_cast<float>(R[j + static_cast<int64_t>(c) * ldr])));
         float inv;
-        const int f = exponent_above(m, &inv);
-        S.colscale[c] = pow2f(f - 8);
-        for (int j0 = 0; j0 < kTcK; j0 += 8) {
-            uint32_t p[kTcSlices][4];
-            for (int u = 0; u < 8; u += 2) {
-                uint32_t lo[kTcSlices], hi[kTcSlices];
-                const int ja = j0 + u, jb = j0 + u + 1;
-                const float xa = (ja < w && c < k) ? static_cast<float>(R[ja + static_cast<int64_t>(c) * ldr]) * inv : 0.0f;
-                const float xb = (jb < w && c < k) ? static_cast<float>(R[jb + static_cast<int64_t>(c) * ldr]) * inv : 0.0f;
-                split3(xa, lo[0], lo[1], lo[2]);
-                split3(xb, hi[0], hi[1], hi[2]);
-                for (int s = 0; s < kTcSlices; ++s) p[s][u / 2] = lo[s] | (hi[s] << 16);
-            }
-            for (int s = 0; s < kTcSlices; ++s)
-                *reinterpret_cast<uint4*>(S.B[s] + core_offset(c, j0)) = make_uint4(p[s][0], p[s][1], p[s][2], p[s][3]);
-        }
+        const int f = exponent_above(__uint_as_float(S.colmax[tid]), &inv);
+        S.colscale[tid] = pow2f(f - 8);
+        S.colinv[tid] = inv;
+    }
+    __syncthreads();
+    for (int e = tid; e < kTcN * kTcK; e += blockDim.x) {
+        const int c = e / kTcK, j = e % kTcK;
+        const float x = (c < k && j < w) ? static_cast<float>(R[j + static_cast<int64_t>(c) * ldr]) * S.colinv[c] : 0.0f;
+        uint32_t sl[kTcSlices];
+        split3(x, sl[0], sl[1], sl[2]);
+        for (int t = 0; t < kTcSlices; ++t)
+            *reinterpret_cast<uint16_t*>(S.B[t] + core_offset(c, j)) = static_cast<uint16_t>(sl[t]);
     }
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
@@ -198,8 +208,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
             const int b = static_cast<int>(i & 1);
             // full[b] too (already complete): orders the producers' row scales before the reads.
-            if (!mbar_wait(&S.tfull[b], static_cast<uint32_t>((i >> 1) & 1)) ||
-                !mbar_wait(&S.full[b], static_cast<uint32_t>((i >> 1) & 1))) {
+            // The warp leaves together (the TMEM loads below are warp-collective).
+            bool ok = mbar_wait(&S.tfull[b], static_cast<uint32_t>((i >> 1) & 1)) &&
+                      mbar_wait(&S.full[b], static_cast<uint32_t>((i >> 1) & 1));
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
                 atomicExch(&S.err, 1);
                 break;
             }
@@ -331,26 +344,362 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (tid == 0 && S.err) atomicExch(error_flag ? error_flag : &g_rotate_tc_error, 1);
 }
 
+// ---------------------------------------------------------------------------
+// FP64 form: out[:, :k] = Q[:, :w] R[:w, :k] in FP64, w, k <= 64.
+//
+// Each FP64 value x of row r becomes the integer X = round(x 2^(1077 - E_r)),
+// E_r the largest biased exponent of the row, so |X| < 2^55, and X is cut into
+// its seven two's-complement bytes X = sum_s a_s 2^(48 - 8 s) (a_0 signed in
+// [-128, 127], a_1..a_6 in [0, 255]); R's columns likewise (exponent F_c,
+// digits b_t). Every digit is exact in BF16 and every digit product in FP32
+// (|a_0 b_t| <= 2^15, |a_s b_t| <= 2^16 otherwise). With
+// acc_d = sum_{s + t = d} sum_j a_s b_t (d <= 6: 28 pairs, seven TMEM
+// accumulators), acc_0..acc_4 stay within 2^24 in magnitude for K <= 64 (the
+// five pairs of d = 4 hold two products of at most 2^15 and three of 2^16) and
+// are exact; acc_5 and acc_6 weigh 2^-40 and 2^-48 relative to acc_0 and may
+// round. The integer
+//   T = 2^24 (acc_0 2^24 + acc_1 2^16 + acc_2 2^8 + acc_3) + acc_4 2^16 + acc_5 2^8 + acc_6
+// is formed in 128-bit arithmetic and rounded once to FP64:
+//   sum_j x_rj R_jc = 2^(E_r + F_c - 2106) T.
+// The parts dropped (pairs with s + t >= 7, bits below the 55th of the row's
+// or column's largest entry) weigh about 2^-55 of |row max| |column max| per
+// term, the level of FP64 rounding in a 57-term dot product.
+//
+// One persistent CTA per SM walks 128-row tiles. Eight producer warps (one
+// thread per row and K-half) read their rows of Q twice: the high words for
+// the row exponent, then the values, written as the seven digit slices in the
+// core-matrix layout; one thread issues the 112 MMAs of a tile (28 pairs x 4
+// K-steps of 16, M = 128, N = 64) and commits them; eight epilogue warps (TMEM
+// lane quarter warp % 4, column half warp / 4) read the accumulators, form T
+// in integers and store FP64 rows. The 112 KB of A slices and the 448 TMEM
+// columns are single-buffered: the producers fill the next tile while the
+// epilogue drains the current one.
+// ---------------------------------------------------------------------------
+constexpr int k64Slices = 7;
+constexpr int k64Acc = 7;
+constexpr int k64EpiWarps = 8, k64ProdWarps = 8;
+constexpr int k64Threads = 32 * (k64EpiWarps + k64ProdWarps + 1);
+
+struct Tc64Smem {
+    alignas(1024) unsigned char A[k64Slices][kTcSliceA];   // 7 x 16 KB
+    alignas(1024) unsigned char B[k64Slices][kTcSliceB];   // 7 x 8 KB
+    int32_t rowexp[2][kTcRows];                             // E_r by tile parity
+    int32_t colexp[kTcN];                                   // F_c
+    alignas(8) unsigned long long full;        // producers -> MMA (A slices written)
+    alignas(8) unsigned long long tfull;       // MMA commit -> epilogue, producers (A free)
+    alignas(8) unsigned long long tempty;      // epilogue -> MMA (TMEM drained)
+    alignas(8) unsigned long long rfull[2];    // producers -> epilogue (row exponents), by tile parity
+    uint32_t tmem;
+    int err;
+};
+
+// Biased exponent field of the double whose high word is hi (sign dropped).
+__device__ __forceinline__ int32_t exp_field(uint32_t hi) { return static_cast<int32_t>((hi >> 20) & 0x7ffu); }
+
+// X = round(x 2^(1077 - emax)) for a double x whose biased exponent is at most
+// emax (so |X| < 2^55); zero and subnormal x give 0. Rounds half away from zero.
+__device__ __forceinline__ long long fixed_point(double x, int32_t emax) {
+    const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
+    const int32_t e = static_cast<int32_t>((bits >> 52) & 0x7ffu);
+    if (e == 0) return 0;
+    const unsigned long long m = (bits & 0xfffffffffffffull) | (1ull << 52);
+    const int32_t d = emax - e;   // >= 0
+    unsigned long long u;
+    if (d <= 2) {
+        u = m << (2 - d);
+    } else {
+        const int32_t s = d - 2;
+        u = s >= 54 ? 0ull : (m + (1ull << (s - 1))) >> s;
+    }
+    const long long v = static_cast<long long>(u);
+    return (bits >> 63) ? -v : v;
+}
+
+// BF16 bit pattern of an integer 0 <= u <= 511 minus `bias` (exact: at most
+// eight significant bits after the subtraction for the ranges used here).
+__device__ __forceinline__ uint32_t bf16_of_int(uint32_t u, float bias) {
+    return __float_as_uint(__int_as_float(0x4B000000 | u) - (8388608.0f + bias)) >> 16;
+}
+
+// The seven digit slices of X as BF16 bit patterns.
+__device__ __forceinline__ void digits7(long long X, uint32_t (&s)[k64Slices]) {
+    const uint32_t lo = static_cast<uint32_t>(X);
+    const int32_t hi = static_cast<int32_t>(X >> 32);
+    s[6] = bf16_of_int(lo & 0xffu, 0.0f);
+    s[5] = bf16_of_int((lo >> 8) & 0xffu, 0.0f);
+    s[4] = bf16_of_int((lo >> 16) & 0xffu, 0.0f);
+    s[3] = bf16_of_int(lo >> 24, 0.0f);
+    s[2] = bf16_of_int(static_cast<uint32_t>(hi) & 0xffu, 0.0f);
+    s[1] = bf16_of_int((static_cast<uint32_t>(hi) >> 8) & 0xffu, 0.0f);
+    s[0] = bf16_of_int(static_cast<uint32_t>((hi >> 16) + 256), 256.0f);   // signed top digit in [-128, 127]
+}
+
+// 2^p T rounded to the nearest FP64 (ties to even), T an exact 128-bit integer.
+__device__ __forceinline__ double scaled_int_to_double(__int128 T, int32_t p) {
+    if (T == 0) return 0.0;
+    const unsigned long long sign = T < 0 ? (1ull << 63) : 0ull;
+    const unsigned __int128 u = static_cast<unsigned __int128>(T < 0 ? -T : T);
+    const unsigned long long uh = static_cast<unsigned long long>(u >> 64);
+    const unsigned long long ul = static_cast<unsigned long long>(u);
+    int32_t top = uh ? 127 - __clzll(static_cast<long long>(uh)) : 63 - __clzll(static_cast<long long>(ul));
+    unsigned long long mant;
+    if (top <= 52) {
+        mant = ul << (52 - top);
+    } else {
+        const int32_t sh = top - 52;
+        mant = static_cast<unsigned long long>(u >> sh);
+        const unsigned __int128 rem = u & ((static_cast<unsigned __int128>(1) << sh) - 1);
+        const unsigned __int128 half = static_cast<unsigned __int128>(1) << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+        if (mant >> 53) {
+            mant >>= 1;
+            ++top;
+        }
+    }
+    const int32_t be = top + p + 1023;
+    if (be <= 0 || be >= 2047) return ldexp(static_cast<double>(T), p);   // outside the normal range
+    return __longlong_as_double(static_cast<long long>(sign | (static_cast<unsigned long long>(be) << 52) |
+                                                       (mant & 0xfffffffffffffull)));
+}
+
+__global__ void __launch_bounds__(k64Threads, 1)
+    rotate_tc64_kernel(const double* Q, int64_t L, int64_t ldq, int32_t w, const double* __restrict__ R, int32_t ldr,
+                       int32_t k, double* out, int64_t ldo, const double* __restrict__ fcol, const double* fnorm,
+                       const int32_t* abort, int32_t* error_flag) {
+    extern __shared__ __align__(1024) unsigned char tc_raw[];
+    Tc64Smem& S = *reinterpret_cast<Tc64Smem*>(tc_raw + ((1024 - (smem_addr(tc_raw) & 1023)) & 1023));
+    if (abort && *abort) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t ntiles = (L + kTcRows - 1) / kTcRows;
+    const int nk = (w + 15) / 16;   // K-steps with data
+
+    // Setup: R's column exponents (a shared maximum) and digit slices, spread
+    // over the whole CTA with consecutive threads on consecutive rows of a column.
+    if (tid < kTcN) S.colexp[tid] = 0;
+    __syncthreads();
+    for (int e = tid; e < kTcN * kTcK; e += blockDim.x) {
+        const int c = e / kTcK, j = e % kTcK;
+        if (c < k && j < w)
+            atomicMax(&S.colexp[c], exp_field(reinterpret_cast<const uint32_t*>(R + j + static_cast<int64_t>(c) * ldr)[1]));
+    }
+    __syncthreads();
+    for (int e = tid; e < kTcN * kTcK; e += blockDim.x) {
+        const int c = e / kTcK, j = e % kTcK;
+        const long long X = (c < k && j < w) ? fixed_point(R[j + static_cast<int64_t>(c) * ldr], S.colexp[c]) : 0;
+        uint32_t sl[k64Slices];
+        digits7(X, sl);
+        for (int t = 0; t < k64Slices; ++t)
+            *reinterpret_cast<uint16_t*>(S.B[t] + core_offset(c, j)) = static_cast<uint16_t>(sl[t]);
+    }
+    if (tid == 0) {
+        mbar_init(&S.full, 32 * k64ProdWarps);
+        mbar_init(&S.tfull, 1);
+        mbar_init(&S.tempty, 32 * k64EpiWarps);
+        mbar_init(&S.rfull[0], 32 * k64ProdWarps / 2);
+        mbar_init(&S.rfull[1], 32 * k64ProdWarps / 2);
+        S.err = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem)),
+                     "r"(2 * kTcAccCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = S.tmem;
+
+    if (warp < k64EpiWarps) {
+        // Epilogue: rows 32 (warp % 4) + lane, columns 32 (warp / 4) .. + 31.
+        const int quarter = warp & 3, half = warp >> 2;
+        const double finv = fcol ? 1.0 / *fnorm : 0.0;
+        int64_t i = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+            const uint32_t par = static_cast<uint32_t>(i & 1);
+            bool ok = mbar_wait(&S.tfull, par) &&
+                      mbar_wait(&S.rfull[i & 1], static_cast<uint32_t>((i >> 1) & 1));
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
+                atomicExch(&S.err, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int row = quarter * 32 + lane;
+            const int64_t r = tile * kTcRows + row;
+            const int32_t er = S.rowexp[i & 1][row];
+            const uint32_t base = tmem + (static_cast<uint32_t>(quarter * 32) << 16);
+            for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 8) {
+                uint32_t v[k64Acc][8];
+#pragma unroll
+                for (int d = 0; d < k64Acc; ++d) {
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                 : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]),
+                                   "=r"(v[d][5]), "=r"(v[d][6]), "=r"(v[d][7])
+                                 : "r"(base + static_cast<uint32_t>(d * kTcN + c0)));
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (r < L) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int c = c0 + j;
+                        if (c < k) {
+                            const int32_t fc = S.colexp[c];
+                            double o;
+                            if (er == 2047 || fc == 2047) {
+                                o = __longlong_as_double(0x7ff8000000000000ll);   // non-finite input
+                            } else {
+                                int32_t a[k64Acc];
+#pragma unroll
+                                for (int d = 0; d < k64Acc; ++d) a[d] = __float2int_rn(__uint_as_float(v[d][j]));
+                                const long long hi = static_cast<long long>(a[0]) * (1ll << 24) +
+                                                     static_cast<long long>(a[1]) * (1ll << 16) +
+                                                     static_cast<long long>(a[2]) * (1ll << 8) + a[3];
+                                const long long lo = static_cast<long long>(a[4]) * (1ll << 16) +
+                                                     static_cast<long long>(a[5]) * (1ll << 8) + a[6];
+                                o = scaled_int_to_double(static_cast<__int128>(hi) * (1ll << 24) + lo, er + fc - 2106);
+                            }
+                            out[r + static_cast<int64_t>(c) * ldo] = o;
+                        }
+                    }
+                }
+            }
+            if (half == 0 && fcol && r < L) out[r + static_cast<int64_t>(k) * ldo] = fcol[r] * finv;
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(&S.tempty);
+        }
+    } else if (warp < k64EpiWarps + k64ProdWarps) {
+        // Producers: row 32 (pw % 4) + lane, K-half pw / 4 (columns 32 kh .. + 31).
+        const int pw = warp - k64EpiWarps;
+        const int row = (pw & 3) * 32 + lane, kh = pw >> 2;
+        int64_t i = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+            // The MMAs of the previous tile have read the A slices.
+            if (i >= 1 && !mbar_wait(&S.tfull, static_cast<uint32_t>((i - 1) & 1))) {
+                atomicExch(&S.err, 1);
+                break;
+            }
+            if (S.err) break;
+            const int64_t r = tile * kTcRows + row;
+            const bool live = r < L;
+            // Row exponent from the high words, all loads issued before use.
+            int32_t emax = 0;
+#pragma unroll
+            for (int j0 = 0; j0 < kTcK; j0 += 16) {
+                uint32_t hw[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u)
+                    hw[u] = (j0 + u < w && live) ? reinterpret_cast<const uint32_t*>(Q + r + static_cast<int64_t>(j0 + u) * ldq)[1]
+                                                 : 0u;
+#pragma unroll
+                for (int u = 0; u < 16; ++u) emax = max(emax, exp_field(hw[u]));
+            }
+            if (kh == 0) S.rowexp[i & 1][row] = emax;
+#pragma unroll 1
+            for (int j0 = kh * 32; j0 < kh * 32 + 32; j0 += 8) {
+                double x[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) x[u] = (j0 + u < w && live) ? Q[r + static_cast<int64_t>(j0 + u) * ldq] : 0.0;
+                uint32_t p[k64Slices][4];
+#pragma unroll
+                for (int u = 0; u < 8; u += 2) {
+                    uint32_t lo[k64Slices], hi[k64Slices];
+                    digits7(fixed_point(x[u], emax), lo);
+                    digits7(fixed_point(x[u + 1], emax), hi);
+#pragma unroll
+                    for (int s = 0; s < k64Slices; ++s) p[s][u / 2] = lo[s] | (hi[s] << 16);
+                }
+#pragma unroll
+                for (int s = 0; s < k64Slices; ++s)
+                    *reinterpret_cast<uint4*>(S.A[s] + core_offset(row, j0)) = make_uint4(p[s][0], p[s][1], p[s][2], p[s][3]);
+            }
+            if (kh == 0) mbar_arrive(&S.rfull[i & 1]);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&S.full);
+        }
+    } else if (lane == 0) {
+        // MMA issue: accumulator d collects the pairs s + t = d.
+        int64_t i = 0;
+        int64_t issued = -1;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+            if (!mbar_wait(&S.full, static_cast<uint32_t>(i & 1))) {
+                atomicExch(&S.err, 1);
+                break;
+            }
+            if (i >= 1 && !mbar_wait(&S.tempty, static_cast<uint32_t>((i - 1) & 1))) {
+                atomicExch(&S.err, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int d = 0; d < k64Acc; ++d) {
+                const uint32_t dcol = tmem + static_cast<uint32_t>(d * kTcN);
+                int first = 1;
+                for (int s = 0; s <= d; ++s) {
+                    const int t = d - s;
+                    for (int kk = 0; kk < nk; ++kk) {
+                        const uint64_t ad = smem_desc(smem_addr(S.A[s]) + kk * 256);
+                        const uint64_t bd = smem_desc(smem_addr(S.B[t]) + kk * 256);
+                        const uint32_t acc = first ? 0u : 1u;
+                        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
+                                     "l"(ad), "l"(bd), "r"(kTcIdesc), "r"(acc));
+                        first = 0;
+                    }
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&S.tfull))
+                         : "memory");
+            issued = i;
+        }
+        if (issued >= 0 && !mbar_wait(&S.tfull, static_cast<uint32_t>(issued & 1))) atomicExch(&S.err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTcAccCols));
+    }
+    if (tid == 0 && S.err) atomicExch(error_flag ? error_flag : &g_rotate_tc_error, 1);
+}
+
 }  // namespace
 
 size_t rotate_tc32_smem_bytes() { return sizeof(TcSmem) + 1024; }
+size_t rotate_tc64_smem_bytes() { return sizeof(Tc64Smem) + 1024; }
 
 static bool g_rotate_tc_ok = false;
+static bool g_rotate_tc64_ok = false;
 static int g_rotate_tc_sms = 0;
+// 1: restart rotations of w, k <= 64 run on the tensor cores (default);
+// 0: on the CUDA cores.
+static int g_rotate_engine = 1;
 
 cudaError_t rotate_tc_configure(size_t max_smem) {
     g_rotate_tc_ok = false;
+    g_rotate_tc64_ok = false;
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess)
         cudaDeviceGetAttribute(&g_rotate_tc_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (max_smem < rotate_tc32_smem_bytes()) return cudaSuccess;
-    const cudaError_t e = cudaFuncSetAttribute(rotate_tc32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               static_cast<int>(rotate_tc32_smem_bytes()));
-    g_rotate_tc_ok = e == cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    if (max_smem >= rotate_tc32_smem_bytes()) {
+        e = cudaFuncSetAttribute(rotate_tc32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(rotate_tc32_smem_bytes()));
+        g_rotate_tc_ok = e == cudaSuccess;
+    }
+    if (e == cudaSuccess && max_smem >= rotate_tc64_smem_bytes()) {
+        e = cudaFuncSetAttribute(rotate_tc64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(rotate_tc64_smem_bytes()));
+        g_rotate_tc64_ok = e == cudaSuccess;
+    }
     return e;
 }
 
 bool rotate_tc32_available() { return g_rotate_tc_ok; }
+bool rotate_tc64_available() { return g_rotate_tc64_ok; }
+void set_rotate_engine(int engine) { g_rotate_engine = engine == 0 ? 0 : 1; }
+int rotate_engine() { return g_rotate_engine; }
 
 int rotate_tc_take_error() {
     int32_t v = 0;
@@ -362,15 +711,27 @@ int rotate_tc_take_error() {
     return v;
 }
 
+static int tc_grid(int64_t L, int sms) {
+    if (sms <= 0) sms = g_rotate_tc_sms > 0 ? g_rotate_tc_sms : 1;
+    const int64_t tiles = (L + kTcRows - 1) / kTcRows;
+    return static_cast<int>(tiles < sms ? tiles : sms);
+}
+
 void launch_rotate_tc32(const float* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
                         float* out, int64_t ldo, const float* fcol, const double* fnorm, const int32_t* abort,
                         int32_t* error_flag, int sms, cudaStream_t stream) {
     if (L <= 0) return;
-    if (sms <= 0) sms = g_rotate_tc_sms > 0 ? g_rotate_tc_sms : 1;
-    const int64_t tiles = (L + kTcRows - 1) / kTcRows;
-    const int grid = static_cast<int>(tiles < sms ? tiles : sms);
-    rotate_tc32_kernel<<<grid, kTcThreads, rotate_tc32_smem_bytes(), stream>>>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol,
-                                                                               fnorm, abort, error_flag);
+    rotate_tc32_kernel<<<tc_grid(L, sms), kTcThreads, rotate_tc32_smem_bytes(), stream>>>(
+        Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, error_flag);
+    count_launch();
+}
+
+void launch_rotate_tc64(const double* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                        double* out, int64_t ldo, const double* fcol, const double* fnorm, const int32_t* abort,
+                        int32_t* error_flag, int sms, cudaStream_t stream) {
+    if (L <= 0) return;
+    rotate_tc64_kernel<<<tc_grid(L, sms), k64Threads, rotate_tc64_smem_bytes(), stream>>>(
+        Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, error_flag);
     count_launch();
 }
 

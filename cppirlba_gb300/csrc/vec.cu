@@ -672,12 +672,30 @@ static bool g_rotate_pipe_ok = false;
 
 template <typename T, typename O>
 void rotate_dispatch(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k, O* out,
-                     int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream) {
+                     int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort, cudaStream_t stream,
+                     bool allow_tc = true) {
     if (w > 128) {
         // Wide bases skip the abort check: the engine only rotates after a
         // restart whose control block it has read (abort clear).
         rotate_wide<T, O>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, stream);
         return;
+    }
+    // Tensor cores (BF16 slice products, FP32 or FP64 accuracy) for the
+    // restart rotations; the CUDA-core kernels below otherwise.
+    if constexpr (std::is_same<T, O>::value) {
+        if (allow_tc && w >= 1 && w <= 64 && k <= 64 && rotate_engine() == 1) {
+            if constexpr (std::is_same<T, float>::value) {
+                if (rotate_tc32_available()) {
+                    launch_rotate_tc32(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, nullptr, 0, stream);
+                    return;
+                }
+            } else {
+                if (rotate_tc64_available()) {
+                    launch_rotate_tc64(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, nullptr, 0, stream);
+                    return;
+                }
+            }
+        }
     }
     if constexpr (std::is_same<T, float>::value && std::is_same<O, float>::value) {
         const bool aligned = ldq % 4 == 0 && ldo % 4 == 0 && reinterpret_cast<uintptr_t>(Q) % 16 == 0 &&
@@ -895,6 +913,14 @@ void launch_rotate(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* 
 }
 
 template <typename T>
+void launch_rotate_cores(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
+                         T* out, int64_t ldo, const T* fcol, const double* fnorm, const int32_t* abort,
+                         cudaStream_t stream) {
+    if (L == 0 || (k == 0 && !fcol)) return;
+    rotate_dispatch<T, T>(Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, stream, false);
+}
+
+template <typename T>
 void launch_rotate_out(const T* Q, int64_t L, int64_t ldq, int32_t w, const double* R, int32_t ldr, int32_t k,
                        double* out, int64_t ldo, cudaStream_t stream) {
     if (L == 0 || k == 0) return;
@@ -990,7 +1016,9 @@ void launch_feature_stats(const DirPlanDev& p, int64_t nobs, int32_t center, int
     template void launch_rotate<T>(const T*, int64_t, int64_t, int32_t, const double*, int32_t, int32_t, T*,        \
                                    int64_t, const T*, const double*, const int32_t*, cudaStream_t);                 \
     template void launch_rotate_out<T>(const T*, int64_t, int64_t, int32_t, const double*, int32_t, int32_t,       \
-                                       double*, int64_t, cudaStream_t);
+                                       double*, int64_t, cudaStream_t);                                             \
+    template void launch_rotate_cores<T>(const T*, int64_t, int64_t, int32_t, const double*, int32_t, int32_t, T*,  \
+                                         int64_t, const T*, const double*, const int32_t*, cudaStream_t);
 IRLBA_INST(float)
 IRLBA_INST(double)
 #undef IRLBA_INST

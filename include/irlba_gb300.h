@@ -259,6 +259,23 @@ irlba_gb300_status irlba_gb300_matrix_set_vector(irlba_gb300_matrix* matrix, con
  * known answers (tests/src/compute.cpp:52-76). */
 irlba_gb300_status irlba_gb300_update_k_device(const int32_t* args, int64_t count, int32_t* out);
 
+/* The restart step's basis rotation (compute.hpp:268-280: V <- V BV,
+ * W <- W BU) on device memory: out[:, :k] = Q[:, :w] R[:w, :k], and
+ * out[:, k] = fcol / *fnorm when fcol is not NULL (fnorm a device pointer).
+ * Q, out and fcol are FP64 (fp64 = 1) or FP32 (fp64 = 0) column-major arrays;
+ * R is FP64; out may be Q. engine 1 runs the tensor-core kernels (BF16 slice
+ * products to FP32 or FP64 accuracy; w, k <= 64, otherwise
+ * IRLBA_GB300_ERROR_UNSUPPORTED), engine 0 the CUDA-core kernels. Returns when
+ * the rotation is complete. Exposed so the rotation kernels can be checked
+ * against each other and an FP64 product. */
+irlba_gb300_status irlba_gb300_rotate_device(int32_t fp64, const void* Q, int64_t L, int64_t ldq, int32_t w,
+                                             const double* R, int32_t ldr, int32_t k, void* out, int64_t ldo,
+                                             const void* fcol, const double* fnorm, int32_t engine, void* stream);
+
+/* Engine of the restart rotations of later compute calls with a working
+ * subspace of at most 64 columns: 1 = tensor cores (default), 0 = CUDA cores. */
+void irlba_gb300_set_rotation_engine(int32_t engine);
+
 /* Stored layout of an undecorated matrix, for byte accounting. */
 irlba_gb300_status irlba_gb300_matrix_layout(const irlba_gb300_matrix* matrix, int64_t* nnz, int32_t* value_bytes,
                                              int32_t* index_bytes_mul, int32_t* index_bytes_adj,
