@@ -1,6 +1,6 @@
 // Batched form: many PCAs of uneven size in one persistent launch.
 //
-// A team of C CTAs (a thread-block cluster; C = 1, 2 or 4) takes one matrix at
+// A team of C CTAs (a thread-block cluster; C = 1, 2, 4 or 8) takes one matrix at
 // a time from a device queue (largest first) and runs its whole centred/scaled
 // PCA: column statistics (pca.hpp:85-109), the IRLBA restart loop of
 // compute.hpp:141-308 with Lanczos bidiagonalization (lanczos.hpp:54-143), full
@@ -65,7 +65,7 @@ struct Persist {
     float RW[kWM * kWM];
     int order[kWM];
     int flags[8];
-    int assign[4];
+    int assign[8];
     int joint;
 };
 constexpr size_t kPersistBytes = (sizeof(Persist) + 127) / 128 * 128;
@@ -682,6 +682,7 @@ cudaError_t batch_configure(size_t max_smem_optin) {
     cudaError_t e = configure_one<1>(want);
     if (e == cudaSuccess) e = configure_one<2>(want);
     if (e == cudaSuccess) e = configure_one<4>(want);
+    if (e == cudaSuccess) e = configure_one<8>(want);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(batch_spmv_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(want));
@@ -707,6 +708,7 @@ int batch_max_teams(int team, size_t smem) {
         }
         case 2: e = cudaOccupancyMaxActiveClusters(&n, batch_pca_kernel<2>, &cfg); break;
         case 4: e = cudaOccupancyMaxActiveClusters(&n, batch_pca_kernel<4>, &cfg); break;
+        case 8: e = cudaOccupancyMaxActiveClusters(&n, batch_pca_kernel<8>, &cfg); break;
         default: break;
     }
     if (e != cudaSuccess) {
@@ -726,6 +728,9 @@ void launch_batch_pca(int team, const BatchProblem* probs, const int32_t* order,
             break;
         case 4:
             batch_pca_kernel<4><<<grid, kBT, smem, stream>>>(probs, order, count, n_joint, prm, results, queue);
+            break;
+        case 8:
+            batch_pca_kernel<8><<<grid, kBT, smem, stream>>>(probs, order, count, n_joint, prm, results, queue);
             break;
         default:
             batch_pca_kernel<1><<<grid, kBT, smem, stream>>>(probs, order, count, n_joint, prm, results, queue);

@@ -351,22 +351,22 @@ struct irlba_gb300_batch {
 
     // Team size and joint prefix for the active matrices (in cost order). A
     // matrix is solved by a whole team when its cost exceeds half of the
-    // average per-CTA load; the rest run one per CTA. The candidate (1, 2 or 4
+    // average per-CTA load; the rest run one per CTA. The candidate (1, 2, 4 or 8
     // CTAs per team) with the smallest estimated makespan
     //   max(largest cost / (team * eff), (joint cost / eff + solo cost) / CTAs)
-    // wins; eff (1, 0.9, 0.8) charges the team barriers.
+    // wins; eff (1, 0.9, 0.8, 0.7) charges the team barriers.
     int choose_team(int32_t active, const std::vector<int64_t>& cost, size_t smem, int* teams_out,
                     int* joint_out) const {
         int best = 1, best_teams = 1, best_joint = 0;
         double best_est = 1e300;
-        const int cands[3] = {1, 2, 4};
-        const double eff[3] = {1.0, 0.9, 0.8};
+        const int cands[4] = {1, 2, 4, 8};
+        const double eff[4] = {1.0, 0.9, 0.8, 0.7};
         int64_t mx = 0, tot = 0;
         for (int i = 0; i < active; ++i) {
             mx = std::max(mx, cost[order[i]]);
             tot += cost[order[i]];
         }
-        for (int c = 0; c < 3; ++c) {
+        for (int c = 0; c < 4; ++c) {
             if (team_request && cands[c] != team_request) continue;
             const int resident = batch_max_teams(cands[c], smem);
             if (resident < 1) continue;
@@ -765,7 +765,8 @@ irlba_gb300_status irlba_gb300_batch_pca(irlba_gb300_batch* b, int32_t center, i
 irlba_gb300_status irlba_gb300_batch_set_team(irlba_gb300_batch* b, int32_t team, int32_t joint) {
     return guarded([&]() {
         if (!b) invalid("batch is NULL");
-        if (team != 0 && team != 1 && team != 2 && team != 4) invalid("team must be 0 (automatic), 1, 2 or 4");
+        if (team != 0 && team != 1 && team != 2 && team != 4 && team != 8)
+            invalid("team must be 0 (automatic), 1, 2, 4 or 8");
         b->team_request = team;
         b->joint_request = joint < 0 ? -1 : joint;
     });

@@ -333,7 +333,7 @@ int64_t batch_stage_limit();
 // Dynamic shared memory of the batched kernels for a given largest staged vector.
 size_t batch_smem_bytes(int64_t max_staged);
 cudaError_t batch_configure(size_t max_smem_optin);
-// Teams of `team` CTAs (a thread-block cluster; 1, 2 or 4) that can be
+// Teams of `team` CTAs (a thread-block cluster; 1, 2, 4 or 8) that can be
 // resident at once with `smem` bytes of dynamic shared memory (0 on error).
 int batch_max_teams(int team, size_t smem);
 // `teams` teams of `team` CTAs take the `count` problems of `order` in turn:

@@ -1,42 +1,42 @@
 // The restart rotation of the FP32 form, out[:, :k] = Q[:, :w] R[:w, :k]
 // (compute.hpp:268-280: V <- V BV, W <- W BU), on the tcgen05 tensor cores.
 //
-// The product keeps FP32 accuracy through error-free BF16 splitting, the
-// scheme of Ozaki, Ogita, Oishi and Rump ("Error-free transformations of
+// FP32 accuracy from BF16 operands by splitting every value into three BF16
+// terms, x = a0 + a1 + a2 exactly (a0 = bf16(x), a1 = bf16(x - a0),
+// a2 = x - a0 - a1: eight significant bits each), as in the error-free
+// splitting of Ozaki, Ogita, Oishi and Rump ("Error-free transformations of
 // matrix multiplication by using fast routines of matrix multiplication",
-// Numerical Algorithms 59, 2012): every row r of Q is scaled by a power of two
-// 2^-e_r with 2^e_r above its largest magnitude and cut into three slices of
-// at most eight significant bits, x 2^-e_r = a0 2^-8 + a1 2^-16 + a2 2^-24 + r
-// with integers |a_s| <= 256 and |r| <= 2^-25 (each slice the nearest integer
-// of the scaled remainder); every column c of R likewise, with 2^-f_c and
-// slices b_t. The slices are exact in BF16 and their products exact in the
-// MMA's FP32 accumulators: |a_s b_t| <= 2^16, a sum over K = 64 stays below
-// 2^22 and the pairs (s, t) with s + t = d (at most three) sum below 2^24. The
-// six pairs with s + t <= 2 are kept (the rest fall below 2^-24 relative), in
-// three TMEM accumulators acc_d, and
-//   out[r, c] = 2^(e_r + f_c - 16) (acc_0 + 2^-8 (acc_1 + 2^-8 acc_2)).
+// Numerical Algorithms 59, 2012), here without exact accumulation: the
+// products a_s b_t are exact in FP32 and the six pairs with s + t <= 2 are
+// added into one FP32 accumulator (smallest pairs first), so the result has
+// the rounding of an FP32 dot product (the dropped pairs weigh 2^-24 and
+// less). R is rounded to FP32 first.
 //
 // One persistent CTA per SM walks 128-row tiles: eight producer warps (two
-// groups of four, alternate tiles, one thread per row) load their rows of Q,
-// find the row exponent and write the three slices to a shared-memory buffer in
-// the no-swizzle K-major core-matrix layout; one thread issues the 24 MMAs of a
-// tile (M = 128, N = 64, K = 16, kind::f16 with BF16 operands and FP32
-// accumulation) and commits them to an mbarrier; four epilogue warps read the
-// three accumulators of their 32 rows from TMEM (tcgen05.ld), combine them and
-// store the output rows. Two slice buffers and two TMEM accumulator sets let
-// the loads and slicing of one tile overlap the MMAs and the epilogue of the
-// previous one. Every wait is bounded: on expiry the CTA records an error,
-// stops issuing work and frees its TMEM.
+// groups of four, alternate tiles, one thread per row) copy their tile of Q
+// into a shared-memory stage with cp.async one tile ahead (or load rows
+// directly when Q is not 16-byte aligned), split it and write the three term
+// slices in the no-swizzle K-major core-matrix layout; one thread issues the
+// 24 MMAs of a tile (M = 128, N = 64, K = 16, kind::f16 with BF16 operands and
+// FP32 accumulation) and commits them to an mbarrier; four epilogue warps read
+// the accumulator of their 32 rows from TMEM (tcgen05.ld) and store the output
+// rows. Two slice buffers and two TMEM accumulators let the loads and
+// splitting of one tile overlap the MMAs and the epilogue of the previous one.
+// Every wait is bounded: on expiry the CTA records an error, stops issuing work
+// and frees its TMEM.
 //
-// The FP64 form's rotation (rotate_tc64_kernel, below) uses the same scheme
-// with seven slices of eight bits taken from an exact fixed-point image of each
-// FP64 value and 28 slice pairs, accurate to the FP64 rounding level.
+// The FP64 form's rotation (rotate_tc64_kernel, below) splits exactly: seven
+// integer slices of eight bits taken from a fixed-point image of each FP64
+// value, 28 slice pairs in exact accumulators, accurate to the FP64 rounding
+// level.
 //
 // Shared-memory layout of a 128 x 64 (or 64 x 64) BF16 operand: core matrices
 // of 8 rows x 16 bytes (eight K-consecutive elements), core (i, kc) at byte
 // (8 i + kc) 128; so the leading byte offset (between K-adjacent cores) is 128
 // and the stride byte offset (between row-adjacent cores) is 1024, and K-step
 // kk of 16 starts 256 kk bytes in.
+
+#include <cuda_bf16.h>
 
 #include <cstdint>
 
@@ -56,7 +56,8 @@ constexpr int kTcN = 64;                                       // padded k = MMA
 constexpr int kTcSlices = 3;
 constexpr uint32_t kTcSliceA = kTcRows * kTcK * 2;             // 16 KB
 constexpr uint32_t kTcSliceB = kTcN * kTcK * 2;                // 8 KB
-constexpr uint32_t kTcAccCols = 256;                           // one accumulator set (3 x 64 used)
+constexpr uint32_t kTcAccCols = 256;                           // TMEM columns per accumulator set (FP64 kernel)
+constexpr uint32_t kTc32Cols = 64;                             // one FP32 accumulator
 constexpr int kTcEpiWarps = 4, kTcProdWarps = 8;
 constexpr int kTcThreads = 32 * (kTcEpiWarps + kTcProdWarps + 1);
 constexpr long long kTcWaitCycles = 4000000000ll;              // bounded waits: about 2 s of SM clock
@@ -64,10 +65,7 @@ constexpr long long kTcWaitCycles = 4000000000ll;              // bounded waits:
 struct TcSmem {
     alignas(1024) unsigned char A[2][kTcSlices][kTcSliceA];
     alignas(1024) unsigned char B[kTcSlices][kTcSliceB];
-    float rowscale[2][kTcRows];
-    float colscale[kTcN];
-    float colinv[kTcN];
-    uint32_t colmax[kTcN];
+    alignas(16) float stage[2][kTcK * kTcRows];   // Q tile per producer group, [column][row]
     alignas(8) unsigned long long full[2];
     alignas(8) unsigned long long tfull[2];
     alignas(8) unsigned long long tempty[2];
@@ -114,37 +112,42 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* b, uint32_t parity
     }
 }
 
-// Nearest integer of y for |y| < 2^22 (adding and removing 1.5 * 2^23).
-__device__ __forceinline__ float round_int(float y) {
-    return __fsub_rn(__fadd_rn(y, 12582912.0f), 12582912.0f);
+// 16-byte asynchronous copy global -> shared; bytes < 16 reads only that many
+// and fills the rest with zeros.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Barrier of the 128 threads of one producer group (named barrier id).
+__device__ __forceinline__ void group_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+// The same barrier, returning whether v holds in every thread of the group.
+__device__ __forceinline__ bool group_all(bool v, int id) {
+    uint32_t r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, 128, p;\n"
+                 " selp.u32 %0, 1, 0, q;\n}\n"
+                 : "=r"(r) : "r"(static_cast<uint32_t>(v)), "r"(id) : "memory");
+    return r != 0;
 }
 
-// The three slices of x (already scaled into (-1, 1)) as BF16 bit patterns.
-__device__ __forceinline__ void split3(float x, uint32_t& s0, uint32_t& s1, uint32_t& s2) {
-    const float y0 = __fmul_rn(x, 256.0f);
-    const float a0 = round_int(y0);
-    const float y1 = __fmul_rn(__fsub_rn(y0, a0), 256.0f);
-    const float a1 = round_int(y1);
-    const float y2 = __fmul_rn(__fsub_rn(y1, a1), 256.0f);
-    const float a2 = round_int(y2);
-    s0 = __float_as_uint(a0) >> 16;
-    s1 = __float_as_uint(a1) >> 16;
-    s2 = __float_as_uint(a2) >> 16;
+// Three-term BF16 split of two values, as packed BF16 pairs (first value in the
+// low half): x = t0 + t1 + t2 exactly for normal x (each term the BF16
+// rounding of the remainder, which is exact in FP32).
+__device__ __forceinline__ void split3x2(float xa, float xb, uint32_t& t0, uint32_t& t1, uint32_t& t2) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(xa, xb);
+    t0 = *reinterpret_cast<uint32_t*>(&h);
+    const float ra = xa - __low2float(h), rb = xb - __high2float(h);
+    h = __floats2bfloat162_rn(ra, rb);
+    t1 = *reinterpret_cast<uint32_t*>(&h);
+    h = __floats2bfloat162_rn(ra - __low2float(h), rb - __high2float(h));
+    t2 = *reinterpret_cast<uint32_t*>(&h);
 }
 
-// 2^e as an FP32 value, -126 <= e <= 127.
-__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
-
-// e with 2^e > m >= 0 (e = 0 for m = 0; rows or columns below 2^-100 are
-// treated as 2^-100 in size), and 2^-e.
-__device__ __forceinline__ int exponent_above(float m, float* inv) {
-    int e = 0;
-    if (m > 0.0f) frexpf(m, &e);   // m = f 2^e, f in [0.5, 1): 2^e > m
-    e = e < -100 ? -100 : e;
-    *inv = pow2f(-e);
-    return e;
-}
-
+// STAGED: Q tiles are copied into shared memory by cp.async one tile ahead
+// (needs a 16-byte aligned Q and ldq % 4 == 0); otherwise each producer
+// thread loads its row directly.
+template <bool STAGED>
 __global__ void __launch_bounds__(kTcThreads, 1)
     rotate_tc32_kernel(const float* Q, int64_t L, int64_t ldq, int32_t w, const double* __restrict__ R, int32_t ldr,
                        int32_t k, float* out, int64_t ldo, const float* __restrict__ fcol, const double* fnorm,
@@ -155,31 +158,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (abort && *abort) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t ntiles = (L + kTcRows - 1) / kTcRows;
+    const int nk = (w + 15) / 16;   // K-steps with data
 
-    // Setup: R's column scales (a shared maximum) and slices, spread over the
-    // whole CTA with consecutive threads on consecutive rows of a column.
-    if (tid < kTcN) S.colmax[tid] = 0u;
-    __syncthreads();
-    for (int e = tid; e < kTcN * kTcK; e += blockDim.x) {
-        const int c = e / kTcK, j = e % kTcK;
-        if (c < k && j < w)
-            atomicMax(&S.colmax[c], __float_as_uint(fabsf(static_cast<float>(R[j + static_cast<int64_t>(c) * ldr]))));
-    }
-    __syncthreads();
-    if (tid < kTcN) {
-        float inv;
-        const int f = exponent_above(__uint_as_float(S.colmax[tid]), &inv);
-        S.colscale[tid] = pow2f(f - 8);
-        S.colinv[tid] = inv;
-    }
-    __syncthreads();
-    for (int e = tid; e < kTcN * kTcK; e += blockDim.x) {
-        const int c = e / kTcK, j = e % kTcK;
-        const float x = (c < k && j < w) ? static_cast<float>(R[j + static_cast<int64_t>(c) * ldr]) * S.colinv[c] : 0.0f;
-        uint32_t sl[kTcSlices];
-        split3(x, sl[0], sl[1], sl[2]);
-        for (int t = 0; t < kTcSlices; ++t)
-            *reinterpret_cast<uint16_t*>(S.B[t] + core_offset(c, j)) = static_cast<uint16_t>(sl[t]);
+    // Setup: R's term slices (R rounded to FP32), spread over the whole CTA
+    // with consecutive threads on consecutive rows of a column, two rows each.
+    for (int e = tid; e < kTcN * kTcK / 2; e += blockDim.x) {
+        const int c = (2 * e) / kTcK, j = (2 * e) % kTcK;
+        const bool live = c < k;
+        const float xa = (live && j < w) ? static_cast<float>(R[j + static_cast<int64_t>(c) * ldr]) : 0.0f;
+        const float xb = (live && j + 1 < w) ? static_cast<float>(R[j + 1 + static_cast<int64_t>(c) * ldr]) : 0.0f;
+        uint32_t t[kTcSlices];
+        split3x2(xa, xb, t[0], t[1], t[2]);
+        for (int q = 0; q < kTcSlices; ++q) *reinterpret_cast<uint32_t*>(S.B[q] + core_offset(c, j)) = t[q];
     }
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
@@ -192,7 +182,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem)),
-                     "r"(2 * kTcAccCols));
+                     "r"(2 * kTc32Cols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -207,10 +197,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         int64_t i = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
             const int b = static_cast<int>(i & 1);
-            // full[b] too (already complete): orders the producers' row scales before the reads.
             // The warp leaves together (the TMEM loads below are warp-collective).
-            bool ok = mbar_wait(&S.tfull[b], static_cast<uint32_t>((i >> 1) & 1)) &&
-                      mbar_wait(&S.full[b], static_cast<uint32_t>((i >> 1) & 1));
+            bool ok = mbar_wait(&S.tfull[b], static_cast<uint32_t>((i >> 1) & 1));
             ok = __all_sync(0xffffffffu, ok);
             if (!ok) {
                 atomicExch(&S.err, 1);
@@ -219,32 +207,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int row = warp * 32 + lane;
             const int64_t r = tile * kTcRows + row;
-            const float rs = S.rowscale[b][row];
-            const uint32_t base = tmem + static_cast<uint32_t>(b) * kTcAccCols + (static_cast<uint32_t>(warp * 32) << 16);
+            const uint32_t base = tmem + static_cast<uint32_t>(b) * kTc32Cols + (static_cast<uint32_t>(warp * 32) << 16);
             for (int c0 = 0; c0 < kTcN; c0 += 16) {
-                uint32_t v[3][16];
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                        "[%16];"
-                        : "=r"(v[d][0]), "=r"(v[d][1]), "=r"(v[d][2]), "=r"(v[d][3]), "=r"(v[d][4]), "=r"(v[d][5]),
-                          "=r"(v[d][6]), "=r"(v[d][7]), "=r"(v[d][8]), "=r"(v[d][9]), "=r"(v[d][10]), "=r"(v[d][11]),
-                          "=r"(v[d][12]), "=r"(v[d][13]), "=r"(v[d][14]), "=r"(v[d][15])
-                        : "r"(base + static_cast<uint32_t>(d * kTcN + c0)));
-                }
+                uint32_t v[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(base + static_cast<uint32_t>(c0)));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 if (r < L) {
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const int c = c0 + j;
-                        if (c < k) {
-                            const float a0 = __uint_as_float(v[0][j]), a1 = __uint_as_float(v[1][j]),
-                                        a2 = __uint_as_float(v[2][j]);
-                            const float s = fmaf(fmaf(a2, 0.00390625f, a1), 0.00390625f, a0);
-                            out[r + static_cast<int64_t>(c) * ldo] = (s * rs) * S.colscale[c];
-                        }
-                    }
+                    for (int j = 0; j < 16; ++j)
+                        if (c0 + j < k) out[r + static_cast<int64_t>(c0 + j) * ldo] = __uint_as_float(v[j]);
                 }
             }
             if (fcol && r < L) out[r + static_cast<int64_t>(k) * ldo] = fcol[r] * finv;
@@ -255,47 +232,68 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         // Producers: group g takes the CTA's tiles i = g, g + 2, ... into buffer g.
         const int pw = warp - kTcEpiWarps;
         const int g = pw / (kTcProdWarps / 2);
-        const int row = (pw % (kTcProdWarps / 2)) * 32 + lane;
+        const int row = (pw % (kTcProdWarps / 2)) * 32 + lane;   // also the thread's index in its group
+        float* stg = S.stage[g];
+        // Copies of tile `tile` into the group's stage: 2,048 16-byte chunks
+        // (4 rows of one column each), 16 per thread, rows past L zero-filled.
+        auto issue = [&](int64_t tile) {
+            const int64_t r0 = tile * kTcRows;
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const int q = row + 128 * u;
+                const int j = q >> 5, r4 = (q & 31) * 4;
+                if (j < w) {
+                    const int64_t rem = L - (r0 + r4);
+                    const uint32_t bytes = rem >= 4 ? 16u : (rem > 0 ? 4u * static_cast<uint32_t>(rem) : 0u);
+                    const float* src = bytes ? Q + r0 + r4 + static_cast<int64_t>(j) * ldq : Q;
+                    cp_async16(stg + j * kTcRows + r4, src, bytes);
+                }
+            }
+            cp_async_commit();
+        };
         int64_t i = g;
-        for (int64_t tile = blockIdx.x + g * static_cast<int64_t>(gridDim.x); tile < ntiles;
-             tile += 2 * static_cast<int64_t>(gridDim.x), i += 2) {
-            if (i >= 2 && !mbar_wait(&S.tempty[g], static_cast<uint32_t>(((i >> 1) - 1) & 1))) {
+        int64_t tile = blockIdx.x + g * static_cast<int64_t>(gridDim.x);
+        if (STAGED && tile < ntiles) issue(tile);
+        for (; tile < ntiles; tile += 2 * static_cast<int64_t>(gridDim.x), i += 2) {
+            const int64_t r = tile * kTcRows + row;
+            float x[kTcK];
+            if (STAGED) {
+                cp_async_wait_all();
+                group_sync(1 + g);          // the whole tile has landed
+#pragma unroll
+                for (int j = 0; j < kTcK; ++j) x[j] = j < w ? stg[j * kTcRows + row] : 0.0f;
+                group_sync(1 + g);          // every thread has read its row
+                const int64_t next = tile + 2 * static_cast<int64_t>(gridDim.x);
+                if (next < ntiles) issue(next);
+            }
+            bool ok = i < 2 || mbar_wait(&S.tempty[g], static_cast<uint32_t>(((i >> 1) - 1) & 1));
+            ok = ok && !S.err;
+            if (STAGED) ok = group_all(ok, 1 + g);   // the group leaves together
+            if (!ok) {
                 atomicExch(&S.err, 1);
                 break;
             }
-            if (S.err) break;
-            const int64_t r = tile * kTcRows + row;
-            float x[kTcK];
-            float m = 0.0f;
+            if (!STAGED) {
 #pragma unroll
-            for (int j = 0; j < kTcK; ++j) {
-                x[j] = (j < w && r < L) ? Q[r + static_cast<int64_t>(j) * ldq] : 0.0f;
-                m = fmaxf(m, fabsf(x[j]));
+                for (int j = 0; j < kTcK; ++j) x[j] = (j < w && r < L) ? Q[r + static_cast<int64_t>(j) * ldq] : 0.0f;
             }
-            float inv;
-            const int e = exponent_above(m, &inv);
-            S.rowscale[g][row] = pow2f(e - 8);
 #pragma unroll
             for (int j0 = 0; j0 < kTcK; j0 += 8) {
                 uint32_t p[kTcSlices][4];
 #pragma unroll
-                for (int u = 0; u < 8; u += 2) {
-                    uint32_t lo[kTcSlices], hi[kTcSlices];
-                    split3(x[j0 + u] * inv, lo[0], lo[1], lo[2]);
-                    split3(x[j0 + u + 1] * inv, hi[0], hi[1], hi[2]);
+                for (int u = 0; u < 8; u += 2) split3x2(x[j0 + u], x[j0 + u + 1], p[0][u / 2], p[1][u / 2], p[2][u / 2]);
 #pragma unroll
-                    for (int s = 0; s < kTcSlices; ++s) p[s][u / 2] = lo[s] | (hi[s] << 16);
-                }
-#pragma unroll
-                for (int s = 0; s < kTcSlices; ++s)
-                    *reinterpret_cast<uint4*>(S.A[g][s] + core_offset(row, j0)) =
-                        make_uint4(p[s][0], p[s][1], p[s][2], p[s][3]);
+                for (int q = 0; q < kTcSlices; ++q)
+                    *reinterpret_cast<uint4*>(S.A[g][q] + core_offset(row, j0)) =
+                        make_uint4(p[q][0], p[q][1], p[q][2], p[q][3]);
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(&S.full[g]);
         }
+        if (STAGED) cp_async_wait_all();   // no copies in flight at exit
     } else if (lane == 0) {
-        // MMA issue: accumulator d of set b collects the pairs s + t = d.
+        // MMA issue: accumulator b collects the pairs s + t = d, d = 2, 1, 0
+        // (smallest terms first), over the K-steps with data.
         int64_t i = 0;
         int64_t issued = -1;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
@@ -309,12 +307,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int d = 0; d < 3; ++d) {
-                const uint32_t dcol = tmem + static_cast<uint32_t>(b) * kTcAccCols + static_cast<uint32_t>(d * kTcN);
-                int first = 1;
+            const uint32_t dcol = tmem + static_cast<uint32_t>(b) * kTc32Cols;
+            int first = 1;
+            for (int d = 2; d >= 0; --d) {
                 for (int s = 0; s <= d; ++s) {
                     const int t = d - s;
-                    for (int kk = 0; kk < kTcK / 16; ++kk) {
+                    for (int kk = 0; kk < nk; ++kk) {
                         const uint64_t ad = smem_desc(smem_addr(S.A[b][s]) + kk * 256);
                         const uint64_t bd = smem_desc(smem_addr(S.B[t]) + kk * 256);
                         const uint32_t acc = first ? 0u : 1u;
@@ -339,7 +337,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTcAccCols));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTc32Cols));
     }
     if (tid == 0 && S.err) atomicExch(error_flag ? error_flag : &g_rotate_tc_error, 1);
 }
@@ -359,7 +357,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // are exact; acc_5 and acc_6 weigh 2^-40 and 2^-48 relative to acc_0 and may
 // round. The integer
 //   T = 2^24 (acc_0 2^24 + acc_1 2^16 + acc_2 2^8 + acc_3) + acc_4 2^16 + acc_5 2^8 + acc_6
-// is formed in 128-bit arithmetic and rounded once to FP64:
+// is formed in 64-bit arithmetic (exactly, or, when |T| >= 2^62 - 2^41, with its
+// low eight bits rounded off first) and rounded once to FP64:
 //   sum_j x_rj R_jc = 2^(E_r + F_c - 2106) T.
 // The parts dropped (pairs with s + t >= 7, bits below the 55th of the row's
 // or column's largest entry) weigh about 2^-55 of |row max| |column max| per
@@ -415,41 +414,41 @@ __device__ __forceinline__ long long fixed_point(double x, int32_t emax) {
     return (bits >> 63) ? -v : v;
 }
 
-// BF16 bit pattern of an integer 0 <= u <= 511 minus `bias` (exact: at most
-// eight significant bits after the subtraction for the ranges used here).
-__device__ __forceinline__ uint32_t bf16_of_int(uint32_t u, float bias) {
-    return __float_as_uint(__int_as_float(0x4B000000 | u) - (8388608.0f + bias)) >> 16;
-}
-
-// The seven digit slices of X as BF16 bit patterns.
-__device__ __forceinline__ void digits7(long long X, uint32_t (&s)[k64Slices]) {
+// The seven digits of X as exact FP32 values (the low four bytes of the low
+// word, the next two bytes and the signed top digit of the high word); the
+// byte u becomes 2^23 + u - 2^23 without a conversion instruction.
+__device__ __forceinline__ void digits7(long long X, float (&f)[k64Slices]) {
     const uint32_t lo = static_cast<uint32_t>(X);
     const int32_t hi = static_cast<int32_t>(X >> 32);
-    s[6] = bf16_of_int(lo & 0xffu, 0.0f);
-    s[5] = bf16_of_int((lo >> 8) & 0xffu, 0.0f);
-    s[4] = bf16_of_int((lo >> 16) & 0xffu, 0.0f);
-    s[3] = bf16_of_int(lo >> 24, 0.0f);
-    s[2] = bf16_of_int(static_cast<uint32_t>(hi) & 0xffu, 0.0f);
-    s[1] = bf16_of_int((static_cast<uint32_t>(hi) >> 8) & 0xffu, 0.0f);
-    s[0] = bf16_of_int(static_cast<uint32_t>((hi >> 16) + 256), 256.0f);   // signed top digit in [-128, 127]
+    const uint32_t hu = static_cast<uint32_t>(hi);
+    f[6] = __int_as_float(0x4B000000 | (lo & 0xffu)) - 8388608.0f;
+    f[5] = __int_as_float(0x4B000000 | ((lo >> 8) & 0xffu)) - 8388608.0f;
+    f[4] = __int_as_float(0x4B000000 | ((lo >> 16) & 0xffu)) - 8388608.0f;
+    f[3] = __int_as_float(0x4B000000 | (lo >> 24)) - 8388608.0f;
+    f[2] = __int_as_float(0x4B000000 | (hu & 0xffu)) - 8388608.0f;
+    f[1] = __int_as_float(0x4B000000 | ((hu >> 8) & 0xffu)) - 8388608.0f;
+    f[0] = __int_as_float(0x4B000000 | static_cast<uint32_t>((hi >> 16) + 256)) - 8388864.0f;   // in [-128, 127]
 }
 
-// 2^p T rounded to the nearest FP64 (ties to even), T an exact 128-bit integer.
-__device__ __forceinline__ double scaled_int_to_double(__int128 T, int32_t p) {
+// Packed BF16 pair of two exact small integers (first in the low half).
+__device__ __forceinline__ uint32_t bf16_pair(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// 2^p T rounded to the nearest FP64 (ties to even), |T| < 2^63 exact.
+__device__ __forceinline__ double scaled_int_to_double(long long T, int32_t p) {
     if (T == 0) return 0.0;
     const unsigned long long sign = T < 0 ? (1ull << 63) : 0ull;
-    const unsigned __int128 u = static_cast<unsigned __int128>(T < 0 ? -T : T);
-    const unsigned long long uh = static_cast<unsigned long long>(u >> 64);
-    const unsigned long long ul = static_cast<unsigned long long>(u);
-    int32_t top = uh ? 127 - __clzll(static_cast<long long>(uh)) : 63 - __clzll(static_cast<long long>(ul));
+    const unsigned long long u = static_cast<unsigned long long>(T < 0 ? -T : T);
+    int32_t top = 63 - __clzll(static_cast<long long>(u));
     unsigned long long mant;
     if (top <= 52) {
-        mant = ul << (52 - top);
+        mant = u << (52 - top);
     } else {
         const int32_t sh = top - 52;
-        mant = static_cast<unsigned long long>(u >> sh);
-        const unsigned __int128 rem = u & ((static_cast<unsigned __int128>(1) << sh) - 1);
-        const unsigned __int128 half = static_cast<unsigned __int128>(1) << (sh - 1);
+        mant = u >> sh;
+        const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
         if (rem > half || (rem == half && (mant & 1ull))) ++mant;
         if (mant >> 53) {
             mant >>= 1;
@@ -460,6 +459,14 @@ __device__ __forceinline__ double scaled_int_to_double(__int128 T, int32_t p) {
     if (be <= 0 || be >= 2047) return ldexp(static_cast<double>(T), p);   // outside the normal range
     return __longlong_as_double(static_cast<long long>(sign | (static_cast<unsigned long long>(be) << 52) |
                                                        (mant & 0xfffffffffffffull)));
+}
+
+// 2^p (hi 2^24 + lo) rounded to FP64, |hi| < 2^47, |lo| < 2^41: exact in
+// 64 bits when |hi| < 2^38; otherwise |value| >= 2^62 - 2^41 and lo's low
+// eight bits (at most 2^-55 of the value) are rounded off first.
+__device__ __forceinline__ double combine_to_double(long long hi, long long lo, int32_t p) {
+    if ((hi < 0 ? -hi : hi) < (1ll << 38)) return scaled_int_to_double(hi * (1ll << 24) + lo, p);
+    return scaled_int_to_double(hi * (1ll << 16) + ((lo + 128) >> 8), p + 8);
 }
 
 __global__ void __launch_bounds__(k64Threads, 1)
@@ -483,13 +490,16 @@ __global__ void __launch_bounds__(k64Threads, 1)
             atomicMax(&S.colexp[c], exp_field(reinterpret_cast<const uint32_t*>(R + j + static_cast<int64_t>(c) * ldr)[1]));
     }
     __syncthreads();
-    for (int e = tid; e < kTcN * kTcK; e += blockDim.x) {
-        const int c = e / kTcK, j = e % kTcK;
-        const long long X = (c < k && j < w) ? fixed_point(R[j + static_cast<int64_t>(c) * ldr], S.colexp[c]) : 0;
-        uint32_t sl[k64Slices];
-        digits7(X, sl);
+    for (int e = tid; e < kTcN * kTcK / 2; e += blockDim.x) {
+        const int c = (2 * e) / kTcK, j = (2 * e) % kTcK;
+        const bool live = c < k;
+        const long long Xa = (live && j < w) ? fixed_point(R[j + static_cast<int64_t>(c) * ldr], S.colexp[c]) : 0;
+        const long long Xb = (live && j + 1 < w) ? fixed_point(R[j + 1 + static_cast<int64_t>(c) * ldr], S.colexp[c]) : 0;
+        float fa[k64Slices], fb[k64Slices];
+        digits7(Xa, fa);
+        digits7(Xb, fb);
         for (int t = 0; t < k64Slices; ++t)
-            *reinterpret_cast<uint16_t*>(S.B[t] + core_offset(c, j)) = static_cast<uint16_t>(sl[t]);
+            *reinterpret_cast<uint32_t*>(S.B[t] + core_offset(c, j)) = bf16_pair(fa[t], fb[t]);
     }
     if (tid == 0) {
         mbar_init(&S.full, 32 * k64ProdWarps);
@@ -558,7 +568,7 @@ __global__ void __launch_bounds__(k64Threads, 1)
                                                      static_cast<long long>(a[2]) * (1ll << 8) + a[3];
                                 const long long lo = static_cast<long long>(a[4]) * (1ll << 16) +
                                                      static_cast<long long>(a[5]) * (1ll << 8) + a[6];
-                                o = scaled_int_to_double(static_cast<__int128>(hi) * (1ll << 24) + lo, er + fc - 2106);
+                                o = combine_to_double(hi, lo, er + fc - 2106);
                             }
                             out[r + static_cast<int64_t>(c) * ldo] = o;
                         }
@@ -604,11 +614,11 @@ __global__ void __launch_bounds__(k64Threads, 1)
                 uint32_t p[k64Slices][4];
 #pragma unroll
                 for (int u = 0; u < 8; u += 2) {
-                    uint32_t lo[k64Slices], hi[k64Slices];
-                    digits7(fixed_point(x[u], emax), lo);
-                    digits7(fixed_point(x[u + 1], emax), hi);
+                    float fa[k64Slices], fb[k64Slices];
+                    digits7(fixed_point(x[u], emax), fa);
+                    digits7(fixed_point(x[u + 1], emax), fb);
 #pragma unroll
-                    for (int s = 0; s < k64Slices; ++s) p[s][u / 2] = lo[s] | (hi[s] << 16);
+                    for (int s = 0; s < k64Slices; ++s) p[s][u / 2] = bf16_pair(fa[s], fb[s]);
                 }
 #pragma unroll
                 for (int s = 0; s < k64Slices; ++s)
@@ -684,8 +694,11 @@ cudaError_t rotate_tc_configure(size_t max_smem) {
         cudaDeviceGetAttribute(&g_rotate_tc_sms, cudaDevAttrMultiProcessorCount, dev);
     cudaError_t e = cudaSuccess;
     if (max_smem >= rotate_tc32_smem_bytes()) {
-        e = cudaFuncSetAttribute(rotate_tc32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(rotate_tc32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(rotate_tc32_smem_bytes()));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(rotate_tc32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(rotate_tc32_smem_bytes()));
         g_rotate_tc_ok = e == cudaSuccess;
     }
     if (e == cudaSuccess && max_smem >= rotate_tc64_smem_bytes()) {
@@ -721,8 +734,13 @@ void launch_rotate_tc32(const float* Q, int64_t L, int64_t ldq, int32_t w, const
                         float* out, int64_t ldo, const float* fcol, const double* fnorm, const int32_t* abort,
                         int32_t* error_flag, int sms, cudaStream_t stream) {
     if (L <= 0) return;
-    rotate_tc32_kernel<<<tc_grid(L, sms), kTcThreads, rotate_tc32_smem_bytes(), stream>>>(
-        Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, error_flag);
+    const bool staged = ldq % 4 == 0 && reinterpret_cast<uintptr_t>(Q) % 16 == 0;
+    if (staged)
+        rotate_tc32_kernel<true><<<tc_grid(L, sms), kTcThreads, rotate_tc32_smem_bytes(), stream>>>(
+            Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, error_flag);
+    else
+        rotate_tc32_kernel<false><<<tc_grid(L, sms), kTcThreads, rotate_tc32_smem_bytes(), stream>>>(
+            Q, L, ldq, w, R, ldr, k, out, ldo, fcol, fnorm, abort, error_flag);
     count_launch();
 }
 

@@ -401,7 +401,7 @@ irlba_gb300_status irlba_gb300_batch_destroy(irlba_gb300_batch* batch);
  * SpMVs per candidate schedule (lanes per row 4/8/16/32 x L2 prefetch
  * distance 0/1/3 row batches) and direction. */
 irlba_gb300_status irlba_gb300_batch_tune(irlba_gb300_batch* batch, int32_t repeats, void* stream);
-/* Teams of CTAs (thread-block clusters of `team` = 1, 2 or 4 CTAs; 0, the
+/* Teams of CTAs (thread-block clusters of `team` = 1, 2, 4 or 8 CTAs; 0, the
  * default, picks per call the size with the smallest estimated makespan). A
  * team solves each of the `joint` largest matrices together and the others
  * one matrix per CTA; joint < 0 (default) picks the matrices whose cost

@@ -48,7 +48,7 @@ def test_batch_matches_oracle(engine, oracle_mod, center, scale):
     init = np.random.default_rng(7).standard_normal(genes)
     b = _batch(engine, inputs)
     st = b.pca(center, scale, 6, engine.Options(initial=init))
-    assert st["single"] == 0 and st["team"] in (1, 2, 4) and st["ctas"] % st["team"] == 0
+    assert st["single"] == 0 and st["team"] in (1, 2, 4, 8) and st["ctas"] % st["team"] == 0
     for j, x in enumerate(inputs):
         res = b.result(j)
         assert res.stats["status"] == engine.BATCH_OK
@@ -62,7 +62,7 @@ def test_batch_matches_oracle(engine, oracle_mod, center, scale):
     b.close()
 
 
-@pytest.mark.parametrize("team,joint", [(1, -1), (2, 5), (4, 5), (4, 2), (4, 0)])
+@pytest.mark.parametrize("team,joint", [(1, -1), (2, 5), (4, 5), (4, 2), (4, 0), (8, 5), (8, 0)])
 def test_batch_team_sizes(engine, oracle_mod, team, joint):
     """Every team size (CTAs per team, a thread-block cluster), with all, some
     or none of the matrices solved jointly, gives the oracle's results, down to

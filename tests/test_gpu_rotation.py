@@ -1,30 +1,33 @@
 """The restart step's basis rotation (compute.hpp:268-280: V <- V BV,
 W <- W BU) on the tensor cores, through the C ABI, against an exact product.
 
-The tensor-core kernels scale every row of Q and column of R by a power of two
-and cut the values into BF16 digit slices (three for the FP32 form, seven for
-FP64) whose products are added in FP32 accumulators; their error is bounded by
-eps (sum_j |Q[r, j]| |R[j, c]| + w max_j |Q[r, j]| max_j |R[j, c]|) with
-eps = 2^-21 (FP32) or 2^-50 (FP64, the level of an FP64 dot product of 64
-terms). The CUDA-core kernels are held to the classical dot-product bound
-(w + 3) u sum_j |Q[r, j]| |R[j, c]| (u = 2^-24 or 2^-53). The exact product is a
-long-double matmul on up to 5,000 of the rows (the first and last 2,000 and a
-random 1,000)."""
+FP64 form: every row of Q and column of R is scaled by a power of two and cut
+into seven exact integer digit slices whose products are summed exactly, so the
+error is bounded by 2^-50 (sum_j |Q[r, j]| |R[j, c]| + w max_j |Q[r, j]|
+max_j |R[j, c]|), the level of an FP64 dot product of 64 terms. FP32 form:
+three-term BF16 splits added into one FP32 accumulator (the rounding of an
+FP32 dot product; each of the 6 slice pairs of each of the 4 K-steps adds once
+to the accumulator): (2 w + 8) u sum_j |Q[r, j]| |R[j, c]|, u = 2^-24. The
+CUDA-core kernels are held to the classical dot-product bound
+(w + 3) u sum_j |Q[r, j]| |R[j, c]| (u = 2^-24 or 2^-53). The exact product is
+a long-double matmul on up to 5,000 of the rows (the first and last 2,000 and
+a random 1,000)."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
-def _rotate(engine, fp64, Q, R, k, engine_id, ldq_pad=0, fcol=None, fnorm=None, inplace=False):
+def _rotate(engine, fp64, Q, R, k, engine_id, ldq_pad=None, fcol=None, fnorm=None, inplace=False):
     """out[:, :k] = Q R[:, :k] (+ out[:, k] = fcol / fnorm) on the GPU; Q is
     L x w (numpy), column-major in device memory with leading dimension
-    L + ldq_pad."""
+    L + ldq_pad, or L rounded up to 32 (the engine's layout, 128-byte aligned
+    columns) when ldq_pad is None."""
     import torch
     lib = engine.load_library()
     L, w = Q.shape
     dt = torch.float64 if fp64 else torch.float32
-    ldq = L + ldq_pad
+    ldq = (L + 31) // 32 * 32 if ldq_pad is None else L + ldq_pad
     cols = max(w, k + 1)
     Qp = np.zeros((cols, ldq))
     Qp[:w, :L] = Q.T
@@ -56,8 +59,12 @@ def _bounds(Q, R, k, fp64, rows):
     ref = (q.astype(np.longdouble) @ r.astype(np.longdouble)).astype(np.float64)
     sigma = np.abs(q) @ np.abs(r)
     mx = np.outer(np.abs(q).max(axis=1), np.abs(r).max(axis=0))
-    eps_tc, u = (2.0 ** -50, 2.0 ** -53) if fp64 else (2.0 ** -21, 2.0 ** -24)
-    return ref, {1: eps_tc * (sigma + w * mx), 0: (w + 3) * u * sigma}
+    if fp64:
+        tc, u = 2.0 ** -50 * (sigma + w * mx), 2.0 ** -53
+    else:
+        u = 2.0 ** -24
+        tc = (2 * w + 8) * u * sigma
+    return ref, {1: tc, 0: (w + 3) * u * sigma}
 
 
 def _check(engine, fp64, Q, R, k, **kw):
@@ -76,14 +83,17 @@ def _orthogonal(w, seed):
 
 
 @pytest.mark.parametrize("fp64", [False, True])
-@pytest.mark.parametrize("L,w,k", [(300001, 57, 50), (5, 3, 2), (4096, 64, 64), (1000, 17, 16), (129, 33, 1)])
-def test_rotation_matches_exact_product(engine, fp64, L, w, k):
+@pytest.mark.parametrize("L,w,k,pad", [(300001, 57, 50, None), (300001, 57, 50, 3), (5, 3, 2, None), (5, 3, 2, 0),
+                                       (4096, 64, 64, None), (1000, 17, 16, 1), (129, 33, 1, None)])
+def test_rotation_matches_exact_product(engine, fp64, L, w, k, pad):
+    # pad None: aligned columns (the FP32 kernel stages tiles with cp.async);
+    # otherwise ldq = L + pad (direct loads).
     rng = np.random.default_rng(L + 7 * w)
     Q = rng.standard_normal((L, w)) / np.sqrt(L)
     if not fp64:
         Q = Q.astype(np.float32).astype(np.float64)
     R = _orthogonal(w, w)
-    _check(engine, fp64, Q, R, k, ldq_pad=3 if L > 1000 else 0)
+    _check(engine, fp64, Q, R, k, ldq_pad=pad)
 
 
 @pytest.mark.parametrize("fp64", [False, True])
