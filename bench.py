@@ -65,6 +65,8 @@ def parse():
                          "launch; adjoint: truncated-SVD forward + backward; csc20k: plain FP64 PCA of the "
                          "20,000-gene x 50,000-cell matrix")
     ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--coding", action="store_true",
+                    help="dictionary-coded values for the FP32 matrix (off by default)")
     ap.add_argument("--spmv-shape", type=int, default=None,
                     help="SpMV launch shape of this run's FP32 matrices (see cppirlba_gb300.set_spmv_shape)")
     return ap.parse_args()
@@ -598,6 +600,8 @@ def main():
     eng.load_library()
     if args.spmv_shape is not None:
         eng.set_spmv_shape(args.spmv_shape)
+    if args.coding:
+        eng.set_value_coding(True)
     t_gen = time.perf_counter()
     inp = make_input(args)
     t_gen = time.perf_counter() - t_gen

@@ -155,6 +155,7 @@ def load_library():
         "irlba_gb300_set_device_ingest": (None, [i32]),
         "irlba_gb300_set_spmv_shape": (None, [i32]),
         "irlba_gb300_set_rotation_engine": (None, [i32]),
+        "irlba_gb300_set_value_coding": (None, [i32]),
         "irlba_gb300_rotate_device": (i32, [i32, P, i64, i64, i32, P, i32, i32, P, i64, P, P, i32, P]),
         "irlba_gb300_set_staging": (None, [i64, i64]),
         "irlba_gb300_last_profile": (None, [pd, ctypes.POINTER(i64)]),
@@ -600,6 +601,13 @@ def set_rotation_engine(engine):
     """Engine of the restart rotations (w, k <= 64) of later compute calls:
     1 = tensor cores (default), 0 = CUDA cores."""
     load_library().irlba_gb300_set_rotation_engine(int(engine))
+
+
+def set_value_coding(on):
+    """Dictionary coding of FP32-form sparse matrices created afterwards: at
+    most 2,048 distinct values are kept as 16-bit codes into a table of the
+    exact values for the products (off by default; results unchanged)."""
+    load_library().irlba_gb300_set_value_coding(int(bool(on)))
 
 
 def set_staging(min_bytes=16 << 20, slice_bytes=8 << 20):

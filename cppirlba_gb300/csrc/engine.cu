@@ -370,6 +370,71 @@ static void build_plan_device(const DevCompressed& h, bool store_f64, bool x_f64
     d.block_seg = plan.block_seg.as<int64_t>();
 }
 
+// ---------------------------------------------------------------------------
+// Dictionary-coded values (off by default). The SpMV moves 6 bytes per FP32
+// entry (value + u16 panel offset); matrices with at most kMaxDict distinct
+// values (count data such as log1p-transformed single-cell counts have a few
+// hundred) can store each value as a u16 code into a dictionary of the exact
+// FP32 values, 4 bytes per entry, decoded from shared memory by the gather.
+// Lossless: products see the stored values bit for bit. The raw values stay
+// for the other kernels (statistics, realization, adjoint products). On the
+// 2,000 x 1.3M bench matrix the coded gather moves a third fewer bytes but is
+// no faster (multiply 0.280 vs 0.284 ms, adjoint 0.309 vs 0.283 ms): the
+// dictionary lookup adds a shared-memory access per entry to a gather whose
+// shared-memory x reads already bound it, so the plain layout stays the default.
+// ---------------------------------------------------------------------------
+static bool g_value_coding = false;
+constexpr int kDictLog2Slots = 12;   // 4,096 hash slots for at most 2,048 values
+
+static void encode_values(BaseMatrix& b, cudaStream_t s) {
+    // FP32 vectors only (the FP64 form stages FP64 panels even for FP32 values).
+    if (!g_value_coding || b.store_f64 || b.form != IRLBA_GB300_FORM_FP32_FP64STEPS) return;
+    DirPlan* plans[2] = {&b.mul, &b.adj};
+    for (DirPlan* p : plans)
+        if (!p->dev.staged || p->dev.nnz == 0 || p->dev.val_f64) return;
+    const int64_t nnz = b.mul.dev.nnz;
+    const size_t nslots = size_t{1} << kDictLog2Slots;
+    DevBuf slots(sizeof(unsigned long long) * nslots), flags(sizeof(uint32_t) * 2);
+    CUDA_TRY(cudaMemsetAsync(slots.ptr, 0, slots.bytes, s));
+    CUDA_TRY(cudaMemsetAsync(flags.ptr, 0, flags.bytes, s));
+    uint32_t* count = flags.as<uint32_t>();
+    int32_t* overflow = reinterpret_cast<int32_t*>(count + 1);
+    launch_dict_insert(static_cast<const float*>(b.mul.dev.val), nnz, slots.as<unsigned long long>(), kDictLog2Slots,
+                       count, overflow, static_cast<uint32_t>(kMaxDict), s);
+    uint32_t hf[2] = {0, 0};
+    CUDA_TRY(d2h_async(hf, flags.ptr, sizeof(hf), s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    if (hf[1] || hf[0] == 0 || hf[0] > static_cast<uint32_t>(kMaxDict)) return;
+    const int32_t ndict = static_cast<int32_t>(hf[0]);
+    DevBuf slot_code(sizeof(uint16_t) * nslots);
+    b.dict.alloc(sizeof(float) * ndict);
+    launch_dict_compact(slots.as<unsigned long long>(), kDictLog2Slots, slot_code.as<uint16_t>(), b.dict.as<float>(),
+                        s);
+    const DeviceInfo& di = device_info();
+    for (DirPlan* p : plans) {
+        DirPlanDev& d = p->dev;
+        p->code.alloc(std::max<size_t>(sizeof(uint16_t) * d.nnz, 16));
+        launch_dict_encode(static_cast<const float*>(d.val), d.nnz, slots.as<unsigned long long>(),
+                           slot_code.as<uint16_t>(), kDictLog2Slots, p->code.as<uint16_t>(), s);
+        d.code = p->code.as<uint16_t>();
+        d.dict = b.dict.as<float>();
+        d.ndict = ndict;
+        d.dict_offset = static_cast<int32_t>((d.panel_width + 3) / 4 * 4);
+        d.smem_bytes = sizeof(float) * (static_cast<size_t>(d.dict_offset) + static_cast<size_t>(ndict));
+        // The coded kernel has its own occupancy: rebalance the CTA ranges for it.
+        const int per_sm = spmv_blocks_per_sm(true, false, false, d.smem_bytes, d.group_lanes, d.shape, true);
+        int64_t nblocks = static_cast<int64_t>(di.sms) * per_sm;
+        const int64_t total_cost = d.nnz + kSegCost * d.nseg;
+        nblocks = std::max<int64_t>(1, std::min<int64_t>(nblocks, std::max<int64_t>(1, total_cost / 2048)));
+        p->block_seg.alloc(sizeof(int64_t) * (nblocks + 1));
+        launch_block_seg(d.segptr, d.nseg, kSegCost, nblocks, p->block_seg.as<int64_t>(), s);
+        d.nblocks = static_cast<int32_t>(nblocks);
+        d.block_seg = p->block_seg.as<int64_t>();
+    }
+    CUDA_TRY(cudaStreamSynchronize(s));
+    CUDA_TRY(cudaGetLastError());
+}
+
 // Stable transpose of a device compressed matrix (entries of each output row
 // in increasing input-row order); hptr: the input pointers on the host, for
 // nnz-balanced chunks of input rows.
@@ -1640,6 +1705,10 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
                 build_plan(trans, base->store_f64, x_f64, base->adj);
             }
         }
+        if (nnz > 0) {
+            StreamGuard sg;
+            encode_values(*base, sg.s);
+        }
         auto* h = new irlba_gb300_matrix();
         h->kind = 0;
         h->base = base;
@@ -1652,6 +1721,8 @@ irlba_gb300_status irlba_gb300_matrix_create_sparse(int64_t nrow, int64_t ncol, 
 
 void irlba_gb300_set_device_ingest(int32_t on) { g_device_ingest = on != 0; }
 void irlba_gb300_set_rotation_engine(int32_t engine) { set_rotate_engine(engine); }
+
+void irlba_gb300_set_value_coding(int32_t on) { g_value_coding = on != 0; }
 
 irlba_gb300_status irlba_gb300_rotate_device(int32_t fp64, const void* Q, int64_t L, int64_t ldq, int32_t w,
                                              const double* R, int32_t ldr, int32_t k, void* out, int64_t ldo,
@@ -1708,6 +1779,10 @@ irlba_gb300_status irlba_gb300_matrix_create_dense(int64_t nrow, int64_t ncol, c
         HostCompressed bycol = dense_to_compressed(nrow, ncol, values, in_f64, ld, row_major != 0, false);
         build_plan(byrow, base->store_f64, x_f64, base->mul);
         build_plan(bycol, base->store_f64, x_f64, base->adj);
+        if (base->mul.dev.nnz > 0) {
+            StreamGuard sg;
+            encode_values(*base, sg.s);
+        }
         auto* h = new irlba_gb300_matrix();
         h->kind = 0;
         h->base = base;
@@ -2144,7 +2219,7 @@ irlba_gb300_status irlba_gb300_matrix_layout(const irlba_gb300_matrix* matrix, i
         require_stored(matrix->base.get(), "matrix_layout");
         const BaseMatrix& A = *matrix->base;
         *nnz = A.mul.dev.nnz;
-        *value_bytes = A.store_f64 ? 8 : 4;
+        *value_bytes = A.store_f64 ? 8 : (A.mul.dev.code ? 2 : 4);
         *index_bytes_mul = A.mul.dev.staged ? 2 : 4;
         *index_bytes_adj = A.adj.dev.staged ? 2 : 4;
         *panels_mul = A.mul.dev.npanels;

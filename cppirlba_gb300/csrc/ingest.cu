@@ -364,4 +364,115 @@ void launch_block_seg(const int64_t* segptr, int64_t nseg, int64_t cost, int64_t
     count_launch();
 }
 
+// ---------------------------------------------------------------------------
+// Value dictionary of an FP32 value array (dictionary-coded SpMV plans): an
+// open-addressing hash set of the values' bit patterns (slot = 1 << 32 | bits,
+// 0 empty; multiplicative hash, linear probing), the compaction of its
+// occupied slots into codes, and the encoding of every entry.
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ uint32_t dict_hash(uint32_t b, int log2h) {
+    return (b * 0x9E3779B1u) >> (32 - log2h);
+}
+
+__global__ void dict_insert_kernel(const float* __restrict__ val, int64_t n, unsigned long long* slots, int log2h,
+                                   uint32_t* count, int32_t* overflow, uint32_t maxd) {
+    const uint32_t hmask = (1u << log2h) - 1;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t b = __float_as_uint(val[i]);
+        const unsigned long long key = (1ull << 32) | b;
+        uint32_t h = dict_hash(b, log2h);
+        bool placed = false;
+        for (uint32_t probe = 0; probe <= hmask; ++probe) {
+            const unsigned long long cur = __ldcg(slots + h);
+            if (cur == key) {
+                placed = true;
+                break;
+            }
+            if (cur == 0ull) {
+                const unsigned long long old = atomicCAS(slots + h, 0ull, key);
+                if (old == 0ull) {
+                    if (atomicAdd(count, 1u) >= maxd) atomicExch(overflow, 1);
+                    placed = true;
+                    break;
+                }
+                if (old == key) {
+                    placed = true;
+                    break;
+                }
+            }
+            h = (h + 1) & hmask;
+        }
+        if (!placed) atomicExch(overflow, 1);
+    }
+}
+
+// One warp: codes of the occupied slots in slot order, and the dictionary.
+__global__ void dict_compact_kernel(const unsigned long long* __restrict__ slots, int log2h, uint16_t* slot_code,
+                                    float* dict) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t nh = 1u << log2h;
+    uint32_t base = 0;
+    for (uint32_t s0 = 0; s0 < nh; s0 += 32) {
+        const unsigned long long v = slots[s0 + lane];
+        const bool occ = v != 0ull;
+        const uint32_t mask = __ballot_sync(0xffffffffu, occ);
+        const uint32_t code = base + __popc(mask & ((1u << lane) - 1u));
+        slot_code[s0 + lane] = static_cast<uint16_t>(occ ? code : 0u);
+        if (occ) dict[code] = __uint_as_float(static_cast<uint32_t>(v));
+        base += __popc(mask);
+    }
+}
+
+// code[i] = the code of val[i]'s slot (every value is in the set); the slots
+// and their codes are staged in shared memory.
+__global__ void dict_encode_kernel(const float* __restrict__ val, int64_t n,
+                                   const unsigned long long* __restrict__ slots,
+                                   const uint16_t* __restrict__ slot_code, int log2h, uint16_t* __restrict__ code) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    const uint32_t nh = 1u << log2h, hmask = nh - 1;
+    unsigned long long* ss = reinterpret_cast<unsigned long long*>(dsm);
+    uint16_t* sc = reinterpret_cast<uint16_t*>(ss + nh);
+    for (uint32_t i = threadIdx.x; i < nh; i += blockDim.x) {
+        ss[i] = slots[i];
+        sc[i] = slot_code[i];
+    }
+    __syncthreads();
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t b = __float_as_uint(val[i]);
+        const unsigned long long key = (1ull << 32) | b;
+        uint32_t h = dict_hash(b, log2h);
+        for (uint32_t probe = 0; probe <= hmask && ss[h] != key; ++probe) h = (h + 1) & hmask;
+        code[i] = sc[h];
+    }
+}
+
+}  // namespace
+
+void launch_dict_insert(const float* val, int64_t n, unsigned long long* slots, int log2h, uint32_t* count,
+                        int32_t* overflow, uint32_t maxd, cudaStream_t s) {
+    if (n <= 0) return;
+    dict_insert_kernel<<<grid_of(n, 152 * 16), kT, 0, s>>>(val, n, slots, log2h, count, overflow, maxd);
+    count_launch();
+}
+
+void launch_dict_compact(const unsigned long long* slots, int log2h, uint16_t* slot_code, float* dict,
+                         cudaStream_t s) {
+    dict_compact_kernel<<<1, 32, 0, s>>>(slots, log2h, slot_code, dict);
+    count_launch();
+}
+
+size_t dict_encode_smem(int log2h) { return (sizeof(unsigned long long) + sizeof(uint16_t)) << log2h; }
+
+void launch_dict_encode(const float* val, int64_t n, const unsigned long long* slots, const uint16_t* slot_code,
+                        int log2h, uint16_t* code, cudaStream_t s) {
+    if (n <= 0) return;
+    dict_encode_kernel<<<grid_of(n, 152 * 4), kT, dict_encode_smem(log2h), s>>>(val, n, slots, slot_code, log2h,
+                                                                                 code);
+    count_launch();
+}
+
 }  // namespace irlba_gb300

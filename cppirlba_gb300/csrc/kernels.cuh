@@ -34,7 +34,16 @@ struct DirPlanDev {
     size_t smem_bytes = 0;
     int32_t group_lanes = 32;            // lanes per segment: 4, 8, 16 or 32
     int32_t shape = 0;                   // launch shape of the kernel (see spmv_shape_threads)
+    // Dictionary-coded values (FP32 staged plans with at most kMaxDict distinct
+    // values): entry i's value is dict[code[i]], the dictionary staged in shared
+    // memory at float offset dict_offset (smem_bytes includes it). NULL: val.
+    const uint16_t* code = nullptr;
+    const float* dict = nullptr;
+    int32_t ndict = 0;
+    int32_t dict_offset = 0;
 };
+// Largest dictionary of a coded plan.
+constexpr int32_t kMaxDict = 2048;
 // Threads per CTA of an SpMV launch shape.
 int spmv_shape_threads(int shape);
 
@@ -70,7 +79,7 @@ void launch_epilogue(T* y, int64_t nrows, const Epilogue<T>& e, const int32_t* a
 
 // Launch configuration helpers (dynamic shared-memory limits, occupancy, grids).
 cudaError_t spmv_configure(size_t max_smem);
-int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group, int shape = 0);
+int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group, int shape = 0, bool coded = false);
 cudaError_t rotate_configure(size_t max_smem);
 // The restart rotations on the tensor cores (rotate_tc.cu): w, k <= 64, FP32
 // (three BF16 slices) and FP64 (seven) forms; out may be Q (rows are read
@@ -283,6 +292,16 @@ void launch_copy_entries(int64_t nnz, const int32_t* idx, const void* val, bool 
                          int32_t* idx32, void* vout, bool out_f64, cudaStream_t s);
 void launch_block_seg(const int64_t* segptr, int64_t nseg, int64_t cost, int64_t nblocks, int64_t* bseg,
                       cudaStream_t s);
+// Value dictionary (ingest.cu): hash set of 2^log2h slots (zeroed by the
+// caller), count of distinct values (overflow set beyond maxd or when full),
+// compaction into codes and dictionary, and the encoding of a value array.
+void launch_dict_insert(const float* val, int64_t n, unsigned long long* slots, int log2h, uint32_t* count,
+                        int32_t* overflow, uint32_t maxd, cudaStream_t s);
+void launch_dict_compact(const unsigned long long* slots, int log2h, uint16_t* slot_code, float* dict,
+                         cudaStream_t s);
+size_t dict_encode_smem(int log2h);
+void launch_dict_encode(const float* val, int64_t n, const unsigned long long* slots, const uint16_t* slot_code,
+                        int log2h, uint16_t* code, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Differentiation form (adjoint.cu). Blocks are row-major FP64 with k <= 64

@@ -14,6 +14,7 @@ namespace irlba_gb300 {
 struct DirPlan {
     DirPlanDev dev;
     DevBuf segptr, idx, val, block_seg;
+    DevBuf code;   // dictionary codes of val (coded plans; val stays for the other kernels)
 };
 
 // A user-defined operator in place of the stored gather plans: its products are
@@ -31,6 +32,7 @@ struct BaseMatrix {
     bool store_f64 = true;
     DirPlan mul;  // rows = nrow, x = ncol
     DirPlan adj;  // rows = ncol, x = nrow
+    DevBuf dict;  // the value dictionary shared by coded plans
     UserOperator op;
     bool is_operator() const { return op.device != nullptr || op.host != nullptr; }
 };

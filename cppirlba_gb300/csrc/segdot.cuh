@@ -118,6 +118,60 @@ __device__ __forceinline__ T segment_dot(const VT* __restrict__ val, const void*
     return (a0 + a1) + (a2 + a3);
 }
 
+// The same for dictionary-coded values: entry i's value is dict[code[i]]
+// (exact: the dictionary holds the stored FP32 values), with u16 codes and u16
+// panel offsets, so one 16-byte vector carries eight entries (4 bytes per
+// entry instead of 6). dict and xs are in shared memory.
+__device__ __forceinline__ void coded_acc(float& acc, const uint4& c, const uint4& i, const float* dict,
+                                          const float* xs) {
+    acc += dict[c.x & 0xffffu] * xs[i.x & 0xffffu];
+    acc += dict[c.x >> 16] * xs[i.x >> 16];
+    acc += dict[c.y & 0xffffu] * xs[i.y & 0xffffu];
+    acc += dict[c.y >> 16] * xs[i.y >> 16];
+    acc += dict[c.z & 0xffffu] * xs[i.z & 0xffffu];
+    acc += dict[c.z >> 16] * xs[i.z >> 16];
+    acc += dict[c.w & 0xffffu] * xs[i.w & 0xffffu];
+    acc += dict[c.w >> 16] * xs[i.w >> 16];
+}
+
+// U vectors per lane in flight per iteration (2 or 4).
+template <int G, int U>
+__device__ __forceinline__ float segment_dot_coded(const uint16_t* __restrict__ code, const uint16_t* __restrict__ idx,
+                                                   const float* dict, const float* xs, int64_t b, int64_t en,
+                                                   int glane) {
+    constexpr int N = 8;
+    float a[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) a[u] = 0.0f;
+    const int64_t head = min(en, (b + (N - 1)) & ~static_cast<int64_t>(N - 1));
+    for (int64_t i = b + glane; i < head; i += G) a[0] += dict[ld_stream(code + i)] * xs[ld_stream(idx + i)];
+    const int64_t q1 = en / N;
+    int64_t q = head / N + glane;
+    const uint4* __restrict__ c4 = reinterpret_cast<const uint4*>(code);
+    const uint4* __restrict__ i4 = reinterpret_cast<const uint4*>(idx);
+    for (; q < q1; q += U * G) {
+        uint4 c[U], ix[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            c[u] = make_uint4(0, 0, 0, 0);
+            ix[u] = make_uint4(0, 0, 0, 0);
+            if (u == 0 || q + u * G < q1) {
+                c[u] = ld_stream(c4 + q + u * G);
+                ix[u] = ld_stream(i4 + q + u * G);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (u == 0 || q + u * G < q1) coded_acc(a[u], c[u], ix[u], dict, xs);
+    }
+    const int64_t t0 = max(head, q1 * N);
+    for (int64_t i = t0 + glane; i < en; i += G) a[U - 1] += dict[ld_stream(code + i)] * xs[ld_stream(idx + i)];
+    float r = 0.0f;
+#pragma unroll
+    for (int u = 0; u < U; ++u) r += a[u];
+    return r;
+}
+
 template <int G, typename T>
 __device__ __forceinline__ T group_sum(T v) {
 #pragma unroll

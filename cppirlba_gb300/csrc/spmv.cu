@@ -112,6 +112,82 @@ __global__ void __launch_bounds__(TH, MINB) spmv_kernel(const DirPlanDev p, cons
     }
 }
 
+// The FP32 staged gather over dictionary-coded values (DirPlanDev::code):
+// the dictionary is staged in shared memory behind the x panel once per CTA,
+// then the same segment walk as spmv_kernel with 8-entry vectors.
+template <int G, int TH, int MINB, int U>
+__global__ void __launch_bounds__(TH, MINB) spmv_coded_kernel(const DirPlanDev p, const float* __restrict__ x,
+                                                                float* __restrict__ y, float* __restrict__ partial,
+                                                                const Epilogue<float> e, const int32_t* abort) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* xs = reinterpret_cast<float*>(smem_raw);
+    float* ds = xs + p.dict_offset;
+    __shared__ unsigned int seg_counter;
+    if (*abort) return;
+    constexpr int kGroups = 32 / G;
+
+    EpiVals<float> ev;
+    ev.beta = e.beta ? static_cast<float>(*e.beta) : 0.0f;
+    ev.alpha = e.alpha ? static_cast<float>(*e.alpha) : 0.0f;
+    for (int i = threadIdx.x; i < p.ndict; i += blockDim.x) ds[i] = p.dict[i];
+
+    const int64_t sb = p.block_seg[blockIdx.x];
+    const int64_t se = p.block_seg[blockIdx.x + 1];
+    const int lane = threadIdx.x & 31;
+    const int group = lane / G, glane = lane % G;
+
+    int64_t s = sb;
+    while (s < se) {
+        const int64_t panel = s / p.nrows;
+        const int64_t pe = min(se, (panel + 1) * p.nrows);
+        __syncthreads();
+        {
+            const int64_t c0 = panel * p.panel_width;
+            const int64_t w = min(p.panel_width, p.ncols - c0);
+            for (int64_t i = threadIdx.x; i < w; i += blockDim.x) {
+                float xv = x[c0 + i];
+                if (e.iscale) xv = e.idivide ? xv / e.iscale[c0 + i] : xv * e.iscale[c0 + i];
+                xs[i] = xv;
+            }
+        }
+        if (threadIdx.x == 0) seg_counter = 0;
+        __syncthreads();
+
+        const unsigned int nhere = static_cast<unsigned int>(pe - s);
+        unsigned int base = 0;
+        if (lane == 0) base = atomicAdd(&seg_counter, static_cast<unsigned int>(kGroups));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        int64_t b = 0, en = 0;
+        if (base + group < nhere) {
+            b = p.segptr[s + base + group];
+            en = p.segptr[s + base + group + 1];
+        }
+        while (base < nhere) {
+            unsigned int next = 0;
+            if (lane == 0) next = atomicAdd(&seg_counter, static_cast<unsigned int>(kGroups));
+            next = __shfl_sync(0xffffffffu, next, 0);
+            int64_t nb = 0, nen = 0;
+            if (next + group < nhere) {
+                nb = p.segptr[s + next + group];
+                nen = p.segptr[s + next + group + 1];
+            }
+            const unsigned int mine = base + group;
+            float acc = 0;
+            if (mine < nhere) acc = segment_dot_coded<G, U>(p.code, p.idx16, ds, xs, b, en, glane);
+            acc = group_sum<G>(acc);
+            if (glane == 0 && mine < nhere) {
+                const int64_t row = s + mine - panel * p.nrows;
+                if (p.npanels == 1) y[row] = apply_epilogue(acc, row, e, ev);
+                else partial[panel * p.nrows + row] = acc;
+            }
+            base = next;
+            b = nb;
+            en = nen;
+        }
+        s = pe;
+    }
+}
+
 template <typename T>
 __global__ void panel_reduce_kernel(const T* __restrict__ partial, int32_t npanels, int64_t nrows, T* __restrict__ y,
                                     const Epilogue<T> e, const int32_t* abort) {
@@ -182,6 +258,28 @@ static void with_spmv_kernel(bool vf64, bool staged, int group, F f, int shape =
 #undef IRLBA_SPMV_G
 }
 
+// Calls f with the coded-value kernel for (group lanes, launch shape).
+template <typename F>
+static void with_coded_kernel(int group, F f, int shape) {
+#define IRLBA_SPMV_C(TH, MB, U)                                  \
+    switch (group) {                                             \
+        case 4: f(spmv_coded_kernel<4, TH, MB, U>); break;       \
+        case 8: f(spmv_coded_kernel<8, TH, MB, U>); break;       \
+        case 16: f(spmv_coded_kernel<16, TH, MB, U>); break;     \
+        default: f(spmv_coded_kernel<32, TH, MB, U>); break;     \
+    }
+    // The coded loop holds eight entries per vector: two vectors in flight per
+    // lane keep the three-per-SM shapes within their 40 registers.
+    if (shape == 1) {
+        IRLBA_SPMV_C(256, 6, 2)
+    } else if (shape == 2) {
+        IRLBA_SPMV_C(512, 3, 2)
+    } else {
+        IRLBA_SPMV_C(256, 1, 4)
+    }
+#undef IRLBA_SPMV_C
+}
+
 int spmv_shape_threads(int shape) { return shape == 2 ? 512 : 256; }
 
 template <typename T>
@@ -191,9 +289,19 @@ void launch_spmv(const DirPlanDev& p, const T* x, T* y, T* partial, const Epilog
     if (p.nblocks > 0) {
         const size_t smem = p.staged ? p.smem_bytes : 0;
         const int th = spmv_shape_threads(p.shape);
-        with_spmv_kernel<T>(p.val_f64 != 0, p.staged != 0, p.group_lanes, [&](auto kernel) {
-            kernel<<<p.nblocks, th, smem, stream>>>(p, x, y, partial, e, abort);
-        }, p.shape);
+        bool coded = false;
+        if constexpr (std::is_same<T, float>::value) {
+            if (p.code) {
+                with_coded_kernel(p.group_lanes, [&](auto kernel) {
+                    kernel<<<p.nblocks, th, smem, stream>>>(p, x, y, partial, e, abort);
+                }, p.shape);
+                coded = true;
+            }
+        }
+        if (!coded)
+            with_spmv_kernel<T>(p.val_f64 != 0, p.staged != 0, p.group_lanes, [&](auto kernel) {
+                kernel<<<p.nblocks, th, smem, stream>>>(p, x, y, partial, e, abort);
+            }, p.shape);
         count_launch();
     }
     if (p.npanels > 1) {
@@ -225,7 +333,13 @@ cudaError_t spmv_configure(size_t max_smem) {
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(max_smem));
     };
+    auto set_coded = [&](auto kernel) {
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(max_smem + sizeof(float) * (kMaxDict + 4)));
+    };
     for (int g = 4; g <= 32; g *= 2) {
+        for (int shape = 0; shape <= 2; ++shape) with_coded_kernel(g, set_coded, shape);
         with_spmv_kernel<float>(false, true, g, set);
         with_spmv_kernel<float>(false, true, g, set, 1);
         with_spmv_kernel<float>(false, true, g, set, 2);
@@ -236,12 +350,16 @@ cudaError_t spmv_configure(size_t max_smem) {
     return err;
 }
 
-int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group, int shape) {
+int spmv_blocks_per_sm(bool staged, bool vf64, bool tf64, size_t smem, int group, int shape, bool coded) {
     int nb = 0;
     const int th = spmv_shape_threads(shape);
     auto occ = [&](auto kernel) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, th, staged ? smem : 0);
     };
+    if (coded) {
+        with_coded_kernel(group, occ, shape);
+        return nb < 1 ? 1 : nb;
+    }
     if (tf64) with_spmv_kernel<double>(vf64, staged, group, occ, shape);
     else with_spmv_kernel<float>(vf64, staged, group, occ, shape);
     return nb < 1 ? 1 : nb;

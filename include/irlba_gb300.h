@@ -276,6 +276,14 @@ irlba_gb300_status irlba_gb300_rotate_device(int32_t fp64, const void* Q, int64_
  * subspace of at most 64 columns: 1 = tensor cores (default), 0 = CUDA cores. */
 void irlba_gb300_set_rotation_engine(int32_t engine);
 
+/* Dictionary coding of FP32-form sparse matrices created afterwards (0, the
+ * default, keeps the plain layout): with 1, a matrix with at most 2,048
+ * distinct values keeps each value as a 16-bit code into a table of the exact
+ * values for the products (4 bytes per entry moved instead of 6; results
+ * unchanged). irlba_gb300_matrix_layout reports value_bytes = 2 for a coded
+ * matrix. */
+void irlba_gb300_set_value_coding(int32_t on);
+
 /* Stored layout of an undecorated matrix, for byte accounting. */
 irlba_gb300_status irlba_gb300_matrix_layout(const irlba_gb300_matrix* matrix, int64_t* nnz, int32_t* value_bytes,
                                              int32_t* index_bytes_mul, int32_t* index_bytes_adj,
