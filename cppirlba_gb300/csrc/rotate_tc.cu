@@ -266,7 +266,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const int64_t next = tile + 2 * static_cast<int64_t>(gridDim.x);
                 if (next < ntiles) issue(next);
             }
-            bool ok = i < 2 || mbar_wait(&S.tempty[g], static_cast<uint32_t>(((i >> 1) - 1) & 1));
+            // Buffer g is free once the MMAs of tile i - 2 have completed (their
+            // commit), independent of that tile's epilogue.
+            bool ok = i < 2 || mbar_wait(&S.tfull[g], static_cast<uint32_t>(((i >> 1) - 1) & 1));
             ok = ok && !S.err;
             if (STAGED) ok = group_all(ok, 1 + g);   // the group leaves together
             if (!ok) {
