@@ -654,7 +654,10 @@ struct Engine {
             return;
         }
         if (col_scale) {
-            if (A.mul.dev.staged) {
+            // FP32: scaled while staging. FP64: scaled once into xtmp (the same
+            // division per entry), so the CTAs that stage the same panel do not
+            // repeat it on the narrow FP64 pipe.
+            if (A.mul.dev.staged && std::is_same<T, float>::value) {
                 e.iscale = svec;
                 e.idivide = ch.scale_divide;
             } else {
@@ -692,7 +695,7 @@ struct Engine {
             return;
         }
         if (row_scale) {
-            if (A.adj.dev.staged) {
+            if (A.adj.dev.staged && std::is_same<T, float>::value) {
                 e.iscale = svec;
                 e.idivide = ch.scale_divide;
             } else {

@@ -609,22 +609,26 @@ __global__ void __launch_bounds__(k64Threads, 1)
             }
             if (kh == 0) S.rowexp[i & 1][row] = emax;
 #pragma unroll 1
-            for (int j0 = kh * 32; j0 < kh * 32 + 32; j0 += 8) {
-                double x[8];
+            for (int j1 = kh * 32; j1 < kh * 32 + 32; j1 += 16) {
+                double x[16];   // sixteen loads in flight per thread
 #pragma unroll
-                for (int u = 0; u < 8; ++u) x[u] = (j0 + u < w && live) ? Q[r + static_cast<int64_t>(j0 + u) * ldq] : 0.0;
-                uint32_t p[k64Slices][4];
+                for (int u = 0; u < 16; ++u) x[u] = (j1 + u < w && live) ? Q[r + static_cast<int64_t>(j1 + u) * ldq] : 0.0;
 #pragma unroll
-                for (int u = 0; u < 8; u += 2) {
-                    float fa[k64Slices], fb[k64Slices];
-                    digits7(fixed_point(x[u], emax), fa);
-                    digits7(fixed_point(x[u + 1], emax), fb);
+                for (int h = 0; h < 16; h += 8) {
+                    uint32_t p[k64Slices][4];
 #pragma unroll
-                    for (int s = 0; s < k64Slices; ++s) p[s][u / 2] = bf16_pair(fa[s], fb[s]);
+                    for (int u = 0; u < 8; u += 2) {
+                        float fa[k64Slices], fb[k64Slices];
+                        digits7(fixed_point(x[h + u], emax), fa);
+                        digits7(fixed_point(x[h + u + 1], emax), fb);
+#pragma unroll
+                        for (int s = 0; s < k64Slices; ++s) p[s][u / 2] = bf16_pair(fa[s], fb[s]);
+                    }
+#pragma unroll
+                    for (int s = 0; s < k64Slices; ++s)
+                        *reinterpret_cast<uint4*>(S.A[s] + core_offset(row, j1 + h)) =
+                            make_uint4(p[s][0], p[s][1], p[s][2], p[s][3]);
                 }
-#pragma unroll
-                for (int s = 0; s < k64Slices; ++s)
-                    *reinterpret_cast<uint4*>(S.A[s] + core_offset(row, j0)) = make_uint4(p[s][0], p[s][1], p[s][2], p[s][3]);
             }
             if (kh == 0) mbar_arrive(&S.rfull[i & 1]);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
