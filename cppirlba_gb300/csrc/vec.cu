@@ -209,10 +209,13 @@ __global__ void __launch_bounds__(kThreads) cgs_update_kernel(const T* __restric
 // The update pass with four FP32 or two FP64 consecutive rows per thread: one
 // 16-byte load per basis column and eight columns in flight, so a warp keeps
 // 4 KB of loads outstanding (the form above keeps 512 B, too few to cover
-// HBM latency at full bandwidth). Each row's products are summed in column
-// order exactly as above, so v is the same; only the norm's partial sums
-// group differently. Needs ldq a multiple of the row count and 16-byte
-// aligned Q and v; rows past the last full group are done by the first CTA.
+// HBM latency at full bandwidth). Columns run from the last to the first: the
+// dot pass just before read the basis column group by column group, so its
+// last columns are the ones still in L2 when this pass starts. Each row's
+// products are therefore summed in descending column order (the form above
+// sums ascending; v differs by rounding only). Needs ldq a multiple of the row
+// count and 16-byte aligned Q and v; rows past the last full group are done by
+// the first CTA.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) cgs_update_vec_kernel(const T* __restrict__ Q, int64_t L, int64_t ldq,
                                                                   int32_t c, const double* __restrict__ t,
@@ -238,16 +241,16 @@ __global__ void __launch_bounds__(kThreads) cgs_update_vec_kernel(const T* __res
 #pragma unroll
         for (int u = 0; u < N; ++u) s[u] = 0;
         const T* __restrict__ q = Q + r;
-        int j = 0;
-        for (; j + 7 < cs; j += 8) {
+        int j = c - 1;
+        for (; j >= cs; --j) vec16_fma<T>(s, *reinterpret_cast<const V*>(q + j * ldq), static_cast<T>(__ldg(t + j)));
+        for (; j >= 7; j -= 8) {
             V x[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) x[u] = *reinterpret_cast<const V*>(q + (j + u) * ldq);
+            for (int u = 0; u < 8; ++u) x[u] = *reinterpret_cast<const V*>(q + (j - u) * ldq);
 #pragma unroll
-            for (int u = 0; u < 8; ++u) vec16_fma<T>(s, x[u], ts[j + u]);
+            for (int u = 0; u < 8; ++u) vec16_fma<T>(s, x[u], ts[j - u]);
         }
-        for (; j < cs; ++j) vec16_fma<T>(s, *reinterpret_cast<const V*>(q + j * ldq), ts[j]);
-        for (; j < c; ++j) vec16_fma<T>(s, *reinterpret_cast<const V*>(q + j * ldq), static_cast<T>(__ldg(t + j)));
+        for (; j >= 0; --j) vec16_fma<T>(s, *reinterpret_cast<const V*>(q + j * ldq), ts[j]);
         V x = *reinterpret_cast<V*>(v + r);
         sq += vec16_update(x, s);
         *reinterpret_cast<V*>(v + r) = x;
