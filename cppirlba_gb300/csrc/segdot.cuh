@@ -105,17 +105,21 @@ __device__ __forceinline__ T segment_dot(const VT* __restrict__ val, const void*
             vd = ld_stream(v4 + q + 3 * G);
             id = ld_stream(i4 + q + 3 * G);
         }
+        // FP64 accumulation (GB300's narrow FP64 pipe): two accumulators, so
+        // combining them costs one add; FP32: four independent chains.
+        constexpr bool kTwo = std::is_same<T, double>::value;
         vec_acc<T, STAGED>(a0, va, ia, g);
         if (hb) vec_acc<T, STAGED>(a1, vb, ib, g);
-        if (hc) vec_acc<T, STAGED>(a2, vc, ic, g);
-        if (hd) vec_acc<T, STAGED>(a3, vd, id, g);
+        if (hc) vec_acc<T, STAGED>(kTwo ? a0 : a2, vc, ic, g);
+        if (hd) vec_acc<T, STAGED>(kTwo ? a1 : a3, vd, id, g);
     }
     const int64_t t0 = max(head, q1 * N);
     if (glane < en - t0) {
         const int64_t i = t0 + glane;
-        a2 += static_cast<T>(ld_stream(val + i)) * g(ld_stream(idx + i));
+        (std::is_same<T, double>::value ? a1 : a2) += static_cast<T>(ld_stream(val + i)) * g(ld_stream(idx + i));
     }
-    return (a0 + a1) + (a2 + a3);
+    if constexpr (std::is_same<T, double>::value) return a0 + a1;
+    else return (a0 + a1) + (a2 + a3);
 }
 
 // The same for dictionary-coded values: entry i's value is dict[code[i]]
