@@ -807,7 +807,9 @@ void run_lanczos_bidiagonalization(const Matrix& mat, LanczosWorkspace& inter, D
 
 // out[:, :k] = Q[:, :w] * R[:, :k]  (the rotation GEMMs of compute.hpp:268,279,302,305).
 // Each output entry sums over j in column order; rows are processed in blocks
-// that stay cache-resident while all k output columns are formed.
+// that stay cache-resident while the output columns are formed four at a time
+// (each loaded row entry of Q feeds four products, as an optimized GEMM's
+// register blocking does; the sums are the same, term by term).
 void rotate(const Dense& Q, const Dense& R, Index k, Dense& out) {
     const Index L = Q.nr, w = Q.nc;
     const int nt = g_dense_threads;
@@ -815,16 +817,27 @@ void rotate(const Dense& Q, const Dense& R, Index k, Dense& out) {
 #pragma omp parallel for num_threads(nt) schedule(static) if (nt > 1 && L > 4096)
     for (Index b = 0; b < nblocks; ++b) {
         const Index r0 = b * kDenseRowBlock, r1 = std::min(L, r0 + kDenseRowBlock), nr = r1 - r0;
-        double acc[kDenseRowBlock];
-        for (Index c = 0; c < k; ++c) {
-            for (Index i = 0; i < nr; ++i) acc[i] = 0;
+        double acc[4][kDenseRowBlock];
+        for (Index c = 0; c < k; c += 4) {
+            const Index cn = std::min<Index>(4, k - c);
+            for (Index u = 0; u < 4; ++u)
+                for (Index i = 0; i < nr; ++i) acc[u][i] = 0;
             for (Index j = 0; j < w; ++j) {
-                const double rj = R(j, c);
                 const double* q = Q.v.data() + j * L + r0;
-                for (Index i = 0; i < nr; ++i) acc[i] += q[i] * rj;
+                const double ra = R(j, c), rb = cn > 1 ? R(j, c + 1) : 0.0, rc = cn > 2 ? R(j, c + 2) : 0.0,
+                             rd = cn > 3 ? R(j, c + 3) : 0.0;
+                for (Index i = 0; i < nr; ++i) {
+                    const double qi = q[i];
+                    acc[0][i] += qi * ra;
+                    acc[1][i] += qi * rb;
+                    acc[2][i] += qi * rc;
+                    acc[3][i] += qi * rd;
+                }
             }
-            double* o = out.v.data() + c * out.nr + r0;
-            for (Index i = 0; i < nr; ++i) o[i] = acc[i];
+            for (Index u = 0; u < cn; ++u) {
+                double* o = out.v.data() + (c + u) * out.nr + r0;
+                for (Index i = 0; i < nr; ++i) o[i] = acc[u][i];
+            }
         }
     }
 }
