@@ -200,8 +200,9 @@ def test_pca_errors(engine):
 
 
 def test_fp32_form_error_vs_fp64_oracle(engine, oracle_mod):
-    """FP32 matrix/basis/matvecs, FP64 steps: singular values within 1e-5 and
-    vectors within 1e-3 of the FP64 oracle on the same (FP32-rounded) input."""
+    """FP32 matrix/basis/matvecs, FP64 steps: singular values within 1e-6
+    (variances within 2e-6) and rotation columns within principal-angle sines of
+    1e-3 of the FP64 oracle on the same (FP32-rounded) input."""
     from cppirlba_gb300 import datagen
     inp = datagen.scrna_pca_input(400, 20000, 0.1, seed=19, dtype=np.float32, cell_major=False)
     init = datagen.start_vector(inp.ncol)
@@ -213,8 +214,8 @@ def test_fp32_form_error_vs_fp64_oracle(engine, oracle_mod):
     orc = oracle_mod.pca(spec, True, True, 10, oracle_mod.options(initial=init), dense_threads=4)
     assert gpu.converged
     rel = np.max(np.abs(gpu.variances - orc["variances"]) / orc["variances"])
-    assert rel < 2e-5
-    assert np.max(column_sines(gpu.rotation, orc["rotation"])) < 1e-2
+    assert rel < 2e-6
+    assert np.max(column_sines(gpu.rotation, orc["rotation"])) < 1e-3
 
 
 def test_fp64_runs_are_bit_reproducible(engine):

@@ -10,8 +10,9 @@ subclass (Matrix/interface.hpp:141-223), whose products the caller supplies.
 
 Each is checked through the C ABI against the oracle on the realized matrix with
 the same start vector: singular values to 1e-10 relative, the same restart
-count and vectors to 1e-8 principal-angle sine in the FP64 form; the FP32 form
-within 2e-5 of the FP64 oracle (the tolerance of the stored-matrix FP32 test).
+count and vectors to 1e-8 principal-angle sine in the FP64 form; in the FP32
+form singular values within 1e-6 and vectors within 1e-3 principal-angle sine
+of the FP64 oracle (the tolerances of the stored-matrix FP32 tests).
 """
 import ctypes
 import os
@@ -97,8 +98,9 @@ def test_host_operator_fp32_form_error_vs_fp64_oracle(engine, oracle_mod):
     gpu = engine.compute(op, 5, engine.Options(initial=init))
     orc = oracle_mod.compute(oracle_mod.Spec.dense(A), 5, oracle_mod.options(initial=init))
     assert gpu.converged
-    assert np.max(np.abs(gpu.D - orc["D"]) / orc["D"]) < 2e-5
-    assert np.max(column_sines(gpu.U, orc["U"])) < 1e-2
+    rel = np.max(np.abs(gpu.D - orc["D"]) / orc["D"])
+    assert rel < 1e-6, rel
+    assert np.max(column_sines(gpu.U, orc["U"])) < 1e-3
 
 
 @pytest.mark.parametrize("shape", [(40, 5), (5, 40)])
@@ -188,8 +190,9 @@ def test_residual_device_operator_matches_oracle(engine, oracle_mod, residual_li
     orc = oracle_mod.compute(oracle_mod.Spec.dense(Rd), 6, oracle_mod.options(initial=init))
     if f32:
         assert gpu.converged
-        assert np.max(np.abs(gpu.D - orc["D"]) / orc["D"]) < 2e-5
-        assert np.max(column_sines(gpu.V, orc["V"])) < 1e-2
+        rel = np.max(np.abs(gpu.D - orc["D"]) / orc["D"])
+        assert rel < 1e-6, rel
+        assert np.max(column_sines(gpu.V, orc["V"])) < 1e-3
     else:
         _assert_fp64_parity(gpu, orc)
         v = np.random.default_rng(33).standard_normal(n)
