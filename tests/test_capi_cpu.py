@@ -200,3 +200,26 @@ def test_python_sparse_input_arrays():
     with pytest.raises(eng.IrlbaError) as e:
         eng.SimpleMatrix(sp.csr_matrix(dense))
     assert e.value.status == eng.ERROR_CUDA
+
+
+def test_rotation_entry_point_checks_arguments_before_the_device():
+    # irlba_gb300_rotate_device validates its arguments on the host: these
+    # calls return their status without touching a GPU.
+    lib = eng.load_library()
+    buf = (ctypes.c_double * 64)()
+    p = ctypes.cast(buf, ctypes.c_void_p)
+    call = lib.irlba_gb300_rotate_device
+    assert call(1, p, -1, 8, 2, p, 2, 2, p, 8, None, None, 1, None) == eng.ERROR_INVALID_ARGUMENT
+    assert call(1, None, 8, 8, 2, p, 2, 2, p, 8, None, None, 1, None) == eng.ERROR_INVALID_ARGUMENT
+    assert call(1, p, 8, 4, 2, p, 2, 2, p, 8, None, None, 1, None) == eng.ERROR_INVALID_ARGUMENT   # ldq < L
+    assert call(1, p, 8, 8, 2, p, 2, 2, p, 8, p, None, 1, None) == eng.ERROR_INVALID_ARGUMENT      # fcol, no fnorm
+    assert call(1, p, 8, 8, 65, p, 65, 2, p, 8, None, None, 1, None) == eng.ERROR_UNSUPPORTED      # w > 64
+    assert call(0, p, 8, 8, 2, p, 2, 65, p, 8, None, None, 1, None) == eng.ERROR_UNSUPPORTED       # k > 64
+    assert "64" in lib.irlba_gb300_last_error().decode()
+
+
+def test_engine_switches_are_exported_and_callable():
+    eng.set_rotation_engine(0)
+    eng.set_rotation_engine(1)
+    eng.set_value_coding(True)
+    eng.set_value_coding(False)
