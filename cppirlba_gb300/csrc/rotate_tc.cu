@@ -440,27 +440,14 @@ __device__ __forceinline__ uint32_t bf16_pair(float a, float b) {
 
 // 2^p T rounded to the nearest FP64 (ties to even), |T| < 2^63 exact.
 __device__ __forceinline__ double scaled_int_to_double(long long T, int32_t p) {
+    // The conversion rounds to nearest (ties to even); the power of two is
+    // then added to the exponent field when the result stays normal.
+    const double d = __ll2double_rn(T);
     if (T == 0) return 0.0;
-    const unsigned long long sign = T < 0 ? (1ull << 63) : 0ull;
-    const unsigned long long u = static_cast<unsigned long long>(T < 0 ? -T : T);
-    int32_t top = 63 - __clzll(static_cast<long long>(u));
-    unsigned long long mant;
-    if (top <= 52) {
-        mant = u << (52 - top);
-    } else {
-        const int32_t sh = top - 52;
-        mant = u >> sh;
-        const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-        if (rem > half || (rem == half && (mant & 1ull))) ++mant;
-        if (mant >> 53) {
-            mant >>= 1;
-            ++top;
-        }
-    }
-    const int32_t be = top + p + 1023;
-    if (be <= 0 || be >= 2047) return ldexp(static_cast<double>(T), p);   // outside the normal range
-    return __longlong_as_double(static_cast<long long>(sign | (static_cast<unsigned long long>(be) << 52) |
-                                                       (mant & 0xfffffffffffffull)));
+    const long long bits = __double_as_longlong(d);
+    const int32_t be = static_cast<int32_t>((bits >> 52) & 0x7ff) + p;
+    if (be <= 0 || be >= 2047) return ldexp(d, p);   // outside the normal range
+    return __longlong_as_double(bits + static_cast<long long>(p) * (1ll << 52));
 }
 
 // 2^p (hi 2^24 + lo) rounded to FP64, |hi| < 2^47, |lo| < 2^41: exact in
