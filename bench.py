@@ -164,6 +164,66 @@ def spmv_alg_bytes(rows, cols, nnz, vec_bytes, val_bytes=4, idx_bytes=4):
     return nnz * (val_bytes + idx_bytes) + (rows + 1) * 8 + (rows + cols) * vec_bytes
 
 
+def solve_alg_bytes(m, n, nnz, steps, restarts, work, s_vec):
+    """Algorithmic bytes of one whole solve, summed over the kernel classes:
+    per Lanczos step one multiply and one adjoint SpMV (int32-index basis) and
+    two CGS calls (W side, length m, and V side, length n: 2 c L s_vec + 3 L
+    s_vec each, c the basis columns at that step); per restart the two
+    rotations ((w + k) L s_vec for V and W). The columns per step and k are not
+    recorded per restart: the first Lanczos run starts from k = 0 and the later
+    ones from the mean k = work - (steps - work) / (restarts - 1)."""
+    spmv = steps * (spmv_alg_bytes(m, n, nnz, s_vec) + spmv_alg_bytes(n, m, nnz, s_vec))
+    later = max(restarts - 1, 0)
+    kbar = work - (steps - work) / later if later else 0.0
+    def run_cols(k):  # sum over j = k .. work - 1 of (j + 1)
+        return (work - k) * (work + k + 1) / 2.0
+    cols = run_cols(0) + later * run_cols(kbar)
+    cgs = 2 * cols * (m + n) * s_vec + 3 * steps * (m + n) * s_vec
+    rot = later * (work + kbar) * (m + n) * s_vec
+    return {"spmv": spmv, "cgs": cgs, "rotation": rot, "total": spmv + cgs + rot}
+
+
+def vendor_spmv_ms(inp, reps=5, device="cuda"):
+    """cuSPARSE CSR SpMV through torch (a vendor reference bar for the gather
+    kernel): best of `reps` products y = A x and y = A^T x on the same FP32
+    matrix, with A^T built on the device by a transpose."""
+    import warnings
+    import torch
+    primary = len(inp.ptr) - 1
+    secondary = inp.nrow if inp.column_major else inp.ncol
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")   # torch's beta-status notice for sparse CSR
+        P = torch.sparse_csr_tensor(torch.tensor(inp.ptr, dtype=torch.int64, device=device),
+                                    torch.tensor(inp.idx, dtype=torch.int64, device=device),
+                                    torch.tensor(inp.val, dtype=torch.float32, device=device),
+                                    size=(primary, secondary))
+        T = P.to_sparse_coo().t().coalesce().to_sparse_csr()
+    A, At = (T, P) if inp.column_major else (P, T)
+    out = {}
+    for name, M in (("multiply", A), ("adjoint", At)):
+        x = torch.randn(M.shape[1], 1, device=device)
+        best = None
+        for _ in range(reps + 1):
+            if device == "cuda":
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                y = torch.sparse.mm(M, x)
+                e1.record()
+                torch.cuda.synchronize()
+                t = e0.elapsed_time(e1)
+            else:
+                t0 = time.perf_counter()
+                y = torch.sparse.mm(M, x)
+                t = (time.perf_counter() - t0) * 1e3
+            best = t if best is None else min(best, t)
+        assert y.shape[0] == M.shape[0]
+        out[name] = best
+    del A, At, P, T
+    if device == "cuda":
+        torch.cuda.empty_cache()
+    return out
+
+
 def make_input(args):
     from cppirlba_gb300 import datagen
     return datagen.scrna_pca_input(args.genes, args.cells, args.density, args.seed, np.float32, cell_major=False)
@@ -732,6 +792,25 @@ def main():
         "clocks": clk,
         "setup_s": {"generate": t_gen, "ingest_fp32": t_ing},
     }
+
+    # Whole solve against the roofline (an estimate: see solve_alg_bytes) and a
+    # vendor bar for the sparse product.
+    try:
+        est = solve_alg_bytes(m, n, nnz, last["stats"]["lanczos_steps"], last["iterations"], NUMBER + 7, 4)
+        out["solve_roofline"] = {"alg_bytes": est, "achieved_gbs": est["total"] / (ms_per_step * 1e-3) / 1e9,
+                                 "frac": est["total"] / (ms_per_step * 1e-3) / 1e9 / peak if peak else None,
+                                 "note": "algorithmic bytes of all SpMV, CGS and rotation launches of one solve "
+                                         "(int32-index basis) / time to tol / measured copy peak"}
+    except Exception as exc:
+        out["solve_roofline"] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+    if rank == 0:
+        try:
+            v = vendor_spmv_ms(inp)
+            out["vendor_spmv_ms"] = {"library": "cuSPARSE CSR SpMV through torch.sparse.mm (FP32, int64 indices)",
+                                     "multiply": v["multiply"], "adjoint": v["adjoint"],
+                                     "this_engine": {"multiply": t_mul, "adjoint": t_adj}}
+        except Exception as exc:
+            out["vendor_spmv_ms"] = {"error": "%s: %s" % (type(exc).__name__, exc)}
 
     # End to end through the public API with host buffers: ingestion (H2D of the
     # compressed matrix), PCA, D2H of scores, rotation and variances.
